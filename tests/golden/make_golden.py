@@ -1,0 +1,142 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference itself.
+
+Run in a checkout that has the reference next to it (default
+``/root/reference``); the fixtures it writes are committed, so the tests never
+need the reference at run time.
+
+* numba flavour (``python/Reconstruction_numba.py`` + ``GPUFuncs_numba.py``):
+  run unmodified with ``GPU: 1`` on the serial CPU stand-in for numba in
+  ``_numba_stub.py``.  Gives ``forward()``, ``backward()`` (flat and curved
+  detectors) and ``Filtering()`` for every filter type.
+* pycuda flavour (``python/Reconstruction_pycuda.py``): run unmodified with the
+  reference's CUDA-C kernels compiled for the host (``oracle/build_ref.py``)
+  behind the pycuda stand-in in ``_pycuda_stub.py``.  Gives ``forward()`` and
+  ``backward()`` with ``ReconCenter`` and ``DetectorOffset`` in play.
+
+Inputs are seeded, so rerunning reproduces the files.
+
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+import copy
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, REPO)
+
+PI = np.pi
+
+
+def base_params(**kw):
+    p = {'SourceInit': [0.0, 100.0, 0.0], 'DetectorInit': [0.0, -50.0, 0.0], 'StartAngle': 0.0,
+         'EndAngle': 2 * PI, 'NumberOfDetectorPixels': [16, 12], 'DetectorPixelSize': [1.0, 1.0],
+         'NumberOfViews': 12, 'ImagePixelSpacing': [0.8, 0.7, 0.9], 'NumberOfImage': [10, 12, 8],
+         'PhantomCenter': [0.0, 0.0, 0.0], 'RotationOrigin': [0.0, 0.0, 0.0], 'ReconCenter': [0.0, 0.0, 0.0],
+         'Method': 'Distance', 'FilterType': 'hann', 'cutoff': 1.0, 'GPU': 1, 'DetectorShape': 'Flat',
+         'Pitch': 0.0}
+    p.update(kw)
+    return p
+
+
+# (name, params, what): what is a subset of {"forward", "backward", "filter"}
+NUMBA_CASES = [
+    ("numba_basic", base_params(), {"forward", "backward", "filter"}),
+    ("numba_offcentre", base_params(PhantomCenter=[0.6, -0.4, 0.3], ReconCenter=[-0.5, 0.35, -0.2],
+                                    StartAngle=0.3, EndAngle=0.3 + PI, NumberOfViews=7,
+                                    NumberOfImage=[9, 11, 6], ImagePixelSpacing=[1.0, 0.9, 1.1]),
+     {"forward", "backward"}),
+    ("numba_helical", base_params(Pitch=0.5, NumberOfViews=10, SourceInit=[0.0, 100.0, 0.5],
+                                  DetectorInit=[0.0, -50.0, 0.5]), {"forward", "backward"}),
+    ("numba_curved", base_params(DetectorShape='Curved', NumberOfViews=9), {"forward", "backward"}),
+    ("numba_fan", base_params(NumberOfDetectorPixels=[24, 1], NumberOfImage=[12, 12, 1],
+                              ImagePixelSpacing=[0.9, 0.9, 1.0], DetectorPixelSize=[1.0, 1.5],
+                              NumberOfViews=16), {"forward", "backward", "filter"}),
+    ("numba_wide", base_params(NumberOfDetectorPixels=[20, 14], DetectorPixelSize=[0.6, 0.7],
+                               NumberOfImage=[12, 10, 9], ImagePixelSpacing=[0.5, 0.55, 0.6],
+                               NumberOfViews=8, StartAngle=0.1, EndAngle=0.1 + 2 * PI), {"forward", "backward"}),
+]
+
+FILTER_TYPES = [('ram-lak', 1.0), ('shepp-logan', 1.0), ('cosine', 1.0), ('hamming', 1.0), ('hann', 1.0),
+                ('hann', 0.5), ('shepp-logan', 0.3)]
+
+PYCUDA_CASES = [
+    ("pycuda_basic", dict(base_params(), DetectorOffset=[0.0, 0.0])),
+    ("pycuda_offset", dict(base_params(ReconCenter=[0.4, -0.3, 0.25], PhantomCenter=[9.0, 9.0, 9.0],
+                                       StartAngle=-0.2, EndAngle=-0.2 + 2 * PI, NumberOfViews=9,
+                                       NumberOfImage=[11, 9, 7]), DetectorOffset=[0.45, -0.3])),
+]
+
+
+def inputs_for(p, seed):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = p['NumberOfImage']
+    nu, nv = p['NumberOfDetectorPixels']
+    image = rng.random((nz, ny, nx), dtype=np.float32)
+    proj = rng.random((p['NumberOfViews'], nv, nu), dtype=np.float32)
+    return image, proj
+
+
+def run_case(Recon, p, image, proj, what):
+    out = {}
+    if "forward" in what:
+        R = Recon(copy.deepcopy(p))
+        R.image = image.copy()
+        R.forward()
+        out["forward"] = np.asarray(R.proj, dtype=np.float32)
+    if "backward" in what:
+        R = Recon(copy.deepcopy(p))
+        R.proj = proj.copy()
+        R.backward()
+        out["backward"] = np.asarray(R.image, dtype=np.float32)
+    return out
+
+
+def main(ref_root):
+    sys.path.insert(0, os.path.join(ref_root, "python"))
+    import _numba_stub
+    _numba_stub.install()
+    import Reconstruction_numba as RN
+
+    from oracle import build_ref
+    lib = build_ref.build(ref_root)
+    import _pycuda_stub
+    _pycuda_stub.install(lib)
+    import Reconstruction_pycuda as RP
+
+    for i, (name, p, what) in enumerate(NUMBA_CASES):
+        t0 = time.time()
+        image, proj = inputs_for(p, 100 + i)
+        out = run_case(RN.Reconstruction, p, image, proj, what)
+        extra = {}
+        if "filter" in what:
+            for ft, cut in FILTER_TYPES:
+                q = dict(p, FilterType=ft, cutoff=cut)
+                R = RN.Reconstruction(copy.deepcopy(q))
+                R.proj = proj.copy()
+                R.Filtering()
+                extra["filter_%s_%g" % (ft, cut)] = np.asarray(R.proj, dtype=np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), params=json.dumps(p), flavour="numba",
+                            image=image, proj=proj, **out, **extra)
+        print("%s: %.1fs %s" % (name, time.time() - t0, sorted(list(out) + list(extra))))
+
+    for i, (name, p) in enumerate(PYCUDA_CASES):
+        t0 = time.time()
+        image, proj = inputs_for(p, 200 + i)
+        out = run_case(RP.Reconstruction, p, image, proj, {"forward", "backward"})
+        R = RP.Reconstruction(copy.deepcopy(p))
+        R.proj = proj.copy()
+        R.Filtering()
+        out["filter_%s_%g" % (p['FilterType'], p['cutoff'])] = np.asarray(R.proj, dtype=np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), params=json.dumps(p), flavour="pycuda",
+                            image=image, proj=proj, **out)
+        print("%s: %.1fs %s" % (name, time.time() - t0, sorted(out)))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
