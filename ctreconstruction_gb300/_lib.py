@@ -1,0 +1,83 @@
+"""ctypes binding of libctgb.so (the C ABI declared in include/ctgb.h).
+
+The library is loaded from the package's in-tree build directory.  There is no
+fallback: if the library is missing, every projector call raises.
+"""
+import ctypes
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libctgb.so")
+
+CTGB_OK = 0
+FLAVOUR_NUMBA = 0
+FLAVOUR_PYCUDA = 1
+FILTER_TYPES = {'ram-lak': 0, 'shepp-logan': 1, 'cosine': 2, 'hamming': 3, 'hann': 4}
+
+
+class CtgbParams(ctypes.Structure):
+    """Mirror of ``ctgb_params`` (include/ctgb.h)."""
+    _fields_ = [("nu", ctypes.c_int32), ("nv", ctypes.c_int32), ("du", ctypes.c_double), ("dv", ctypes.c_double),
+                ("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("nviews", ctypes.c_int32), ("start_angle", ctypes.c_double), ("end_angle", ctypes.c_double),
+                ("source_init", ctypes.c_double * 3), ("detector_init", ctypes.c_double * 3),
+                ("rotation_origin", ctypes.c_double * 3), ("phantom_center", ctypes.c_double * 3),
+                ("recon_center", ctypes.c_double * 3), ("detector_offset", ctypes.c_double * 2),
+                ("pitch", ctypes.c_double), ("curved", ctypes.c_int32), ("flavour", ctypes.c_int32)]
+
+
+# (name, argtypes); every entry point returns int status except the string getters.
+_P = ctypes.POINTER(CtgbParams)
+_vp, _i32, _f32, _sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float, ctypes.c_size_t
+SIGNATURES = {
+    "ctgb_table_bytes": [_P, ctypes.POINTER(_sz)],
+    "ctgb_table_build": [_P, _vp, _sz],
+    "ctgb_forward": [_P, _vp, _vp, _vp, _vp, _i32, _i32, _vp],
+    "ctgb_transpose_xy": [_vp, _vp, _i32, _i32, _i32, _vp],
+    "ctgb_backproject_fdk": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
+    "ctgb_backproject_matched": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
+    "ctgb_filter_bytes": [_P, ctypes.POINTER(_sz)],
+    "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],
+    "ctgb_fdk_filter": [_P, _vp, _vp, _i32, _vp],
+}
+STRING_FUNCS = ("ctgb_last_error", "ctgb_version")
+
+_lib = None
+
+
+class CtgbError(RuntimeError):
+    pass
+
+
+def load():
+    """Load libctgb.so (building it first if this checkout has not yet)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build as _build
+        _build.build()
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    for name in STRING_FUNCS:
+        fn = getattr(lib, name)
+        fn.argtypes = []
+        fn.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+def call(name, *args):
+    """Call an entry point; raise ValueError/CtgbError on a non-zero status."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != CTGB_OK:
+        msg = lib.ctgb_last_error().decode()
+        if st in (-1, -3):
+            raise ValueError("%s: %s" % (name, msg))
+        raise CtgbError("%s failed (%d): %s" % (name, st, msg))
+    return st

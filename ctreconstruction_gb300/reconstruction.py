@@ -1,0 +1,123 @@
+"""Drop-in ``Reconstruction`` class: the call surface of the reference's
+``Reconstruction`` (python/Reconstruction_numba.py:55-1614 and
+python/Reconstruction_pycuda.py:62-1513) on top of the GB300 projectors.
+
+``image`` is ``[nz, ny, nx]`` float32 and ``proj`` is ``[nViews, nv, nu]``
+float32, as in the reference.  Either may be a NumPy array (results come back
+as NumPy, like the reference) or a CUDA tensor (results stay on the device, no
+host round trip).  All arithmetic runs in libctgb's CUDA kernels.
+"""
+import numpy as np
+import torch
+
+from .geometry import ReconstructionParams
+from .projector import Projector
+
+
+class ErrorDescription(Exception):
+    """Error codes of the reference (Reconstruction_numba.py:36-52)."""
+    _MSG = {1: 'Unknown variables', 2: 'Unknown data precision',
+            3: 'Number of file is different from number of projection data required',
+            4: 'Cutoff have to be pose between 0 and 0.5', 5: 'Smooth have to be pose between 0 and 1'}
+
+    def __init__(self, value):
+        self.msg = self._MSG.get(value, 'Unknown error')
+        super().__init__(self.msg)
+
+    def __str__(self):
+        return self.msg
+
+
+def _to_device(a, device):
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device, dtype=torch.float32)
+        return t.contiguous()
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(device, non_blocking=False)
+
+
+class Reconstruction:
+    def __init__(self, params, flavour=None, device=None):
+        self.p = ReconstructionParams.from_dict(params, flavour)
+        self.params = self.p.as_dict()
+        p = self.p
+        self.nu, self.nv = p.NumberOfDetectorPixels
+        self.du, self.dv = p.DetectorPixelSize
+        self.nx, self.ny, self.nz = p.NumberOfImage
+        self.dx, self.dy, self.dz = p.ImagePixelSpacing
+        self.Origin = np.array(p.RotationOrigin)
+        self.PhantomCenter = np.array(p.PhantomCenter)
+        self.ReconCenter = p.ReconCenter
+        self.cutoff = p.cutoff
+        self.DetectorShape = p.DetectorShape
+        self.P = p.Pitch
+        self.Source = np.array(p.SourceInit, dtype=np.float64)
+        self.Detector = np.array(p.DetectorInit, dtype=np.float64)
+        self.SAD = p.sad
+        self.SDD = p.sdd
+        self.HelicalTrans = self.P * (self.nv * self.dv) * self.SAD / self.SDD
+        self.nView = p.NumberOfViews
+        self.sAngle, self.eAngle = p.StartAngle, p.EndAngle
+        self.Method = p.Method
+        self.FilterType = p.FilterType
+        self.DetectorOffset = p.DetectorOffset
+        self.GPU = True
+        self.projector = Projector(p, device=device)
+        self.image = None
+        self.proj = None
+
+    # -- raw float32 I/O (Reconstruction_numba.py:92-104) ------------------------
+    def LoadProj(self, filename, dtype=np.float32):
+        self.proj = np.fromfile(filename, dtype=dtype).reshape([self.nView, self.nv, self.nu])
+
+    def LoadRecon(self, filename, dtype=np.float32):
+        self.image = np.fromfile(filename, dtype=dtype).reshape([self.nz, self.ny, self.nx])
+
+    def SaveProj(self, filename):
+        _host(self.proj).tofile(filename, sep='', format='')
+
+    def SaveRecon(self, filename):
+        _host(self.image).tofile(filename, sep='', format='')
+
+    def FlipProj(self, dir):
+        """dir 0 flips each view along v, 1 along u (Reconstruction_numba.py:106-119)."""
+        if dir not in (0, 1):
+            print(ErrorDescription(4))
+            return
+        axis = 1 if dir == 0 else 2
+        if isinstance(self.proj, torch.Tensor):
+            self.proj = torch.flip(self.proj, dims=[axis]).contiguous()
+        else:
+            self.proj = np.ascontiguousarray(np.flip(self.proj, axis=axis))
+
+    # -- projectors ----------------------------------------------------------------
+    def forward(self):
+        """self.proj = DD forward projection of self.image (distance_forward)."""
+        if self.Method != 'Distance':
+            return
+        host = not isinstance(self.image, torch.Tensor)
+        vol = _to_device(self.image, self.projector.device)
+        proj = self.projector.forward(vol)
+        self.proj = _host(proj) if host else proj
+
+    def backward(self):
+        """self.image = FDK-weighted DD backprojection of self.proj * dtheta
+        (distance_backproj)."""
+        if self.Method != 'Distance':
+            return
+        host = not isinstance(self.proj, torch.Tensor)
+        q = _to_device(self.proj, self.projector.device)
+        vol = self.projector.backproject_fdk(q)
+        self.image = _host(vol) if host else vol
+
+    def Filtering(self):
+        """In-place cosine pre-weight and ramp filter of self.proj (Filtering)."""
+        host = not isinstance(self.proj, torch.Tensor)
+        q = _to_device(self.proj, self.projector.device)
+        self.projector.filter(q, self.FilterType, self.cutoff)
+        self.proj = _host(q) if host else q
+
+
+def _host(a):
+    if isinstance(a, torch.Tensor):
+        return a.detach().to("cpu").numpy()
+    return a

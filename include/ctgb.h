@@ -1,0 +1,111 @@
+/* ctgb.h — C ABI of the GB300 CT projection library (libctgb.so).
+ *
+ * Plain C: pointers, sizes, status codes.  Device pointers are CUDA global
+ * memory owned by the caller; `stream` is a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  No entry point allocates device memory,
+ * synchronises the device or exits the process.  Every entry point returns
+ * CTGB_OK or a negative status; ctgb_last_error() gives the message of the
+ * calling thread's last failure.
+ *
+ * Array layouts follow the reference (leehoy/CTReconstruction):
+ *   volume      float32 [nz][ny][nx]      (Reconstruction.image)
+ *   projections float32 [nviews][nv][nu]  (Reconstruction.proj)
+ * y and z voxel indices run from +y/+z to -y/-z and detector rows from +z to
+ * -z, as in python/Reconstruction_numba.py:813-815.
+ */
+#ifndef CTGB_H
+#define CTGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTGB_OK 0
+#define CTGB_ERR_ARG (-1)      /* invalid argument / geometry                 */
+#define CTGB_ERR_CUDA (-2)     /* CUDA launch or runtime error                */
+#define CTGB_ERR_SIZE (-3)     /* buffer too small / size out of range        */
+#define CTGB_ERR_TIMEOUT (-4)  /* a bounded device wait ran out               */
+
+#define CTGB_FLAVOUR_NUMBA 0   /* python/Reconstruction_numba.py conventions  */
+#define CTGB_FLAVOUR_PYCUDA 1  /* python/Reconstruction_pycuda.py conventions */
+
+/* Scan geometry: the reference's params dict (Reconstruction_numba.py:58-62,
+ * Reconstruction_pycuda.py:65-70), one field per key. */
+typedef struct ctgb_params {
+    int32_t nu, nv;                 /* NumberOfDetectorPixels                    */
+    double du, dv;                  /* DetectorPixelSize                         */
+    int32_t nx, ny, nz;             /* NumberOfImage                             */
+    double dx, dy, dz;              /* ImagePixelSpacing                         */
+    int32_t nviews;                 /* NumberOfViews                             */
+    double start_angle, end_angle;  /* StartAngle, EndAngle (views: linspace(s,e,n+1)[:-1]) */
+    double source_init[3];          /* SourceInit                                */
+    double detector_init[3];        /* DetectorInit                              */
+    double rotation_origin[3];      /* RotationOrigin                            */
+    double phantom_center[3];       /* PhantomCenter                             */
+    double recon_center[3];         /* ReconCenter                               */
+    double detector_offset[2];      /* DetectorOffset (pycuda flavour only)      */
+    double pitch;                   /* Pitch (helical)                           */
+    int32_t curved;                 /* DetectorShape: 0 'Flat', 1 'Curved'       */
+    int32_t flavour;                /* CTGB_FLAVOUR_*                            */
+} ctgb_params;
+
+/* ---- geometry tables -------------------------------------------------------
+ * The per-view geometry the reference recomputes in NumPy on every call
+ * (distance_forward Reconstruction_numba.py:834-908; distance_backproj
+ * :405-413) is built once, in float64 on the host, into a flat table that the
+ * caller copies to device memory and passes to the projectors. */
+int ctgb_table_bytes(const ctgb_params *p, size_t *bytes);
+int ctgb_table_build(const ctgb_params *p, void *host_table, size_t bytes);
+
+/* ---- DD forward projection -------------------------------------------------
+ * Replaces Reconstruction.forward()/distance_forward (Reconstruction_numba.py
+ * :793-1117) and the kernels distance_project_on_{x,y,z}
+ * (GPUFuncs_numba.py:88-240; GPUFuncs_pycuda.py:398-588, *_3 variants).
+ * proj[v-view0] = A vol for views [view0, view0+nviews).  vol_xzy is optional
+ * (may be NULL): a copy of vol in [nz][nx][ny] order (ctgb_transpose_xy) that
+ * lets x-dominant views read the volume with unit stride.  proj is
+ * overwritten.  Stream-ordered; no synchronisation. */
+int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
+                 float *d_proj, int32_t view0, int32_t nviews, void *stream);
+
+/* vol_xzy[z][x][y] = vol[z][y][x]. */
+int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t ny, int32_t nz, void *stream);
+
+/* ---- FDK-weighted DD backprojection ---------------------------------------
+ * Replaces Reconstruction.backward()/distance_backproj (Reconstruction_numba.py
+ * :261-271, :371-482) and flat_/curved_distance_backproj_arb
+ * (GPUFuncs_numba.py:391-686; GPUFuncs_pycuda.py:837-956 flat_..._arb2).
+ * vol = (accumulate ? vol : 0) + scale * sum_v BP_v(proj[v-view0]) where the
+ * reference's backward() uses scale = dtheta = angle[1]-angle[0]. */
+int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                         int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
+
+/* ---- matched DD backprojection (exact adjoint of ctgb_forward) -------------
+ * No reference counterpart (the reference's backward() is FDK-weighted);
+ * vol = (accumulate ? vol : 0) + scale * A^T proj. */
+int ctgb_backproject_matched(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                             int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
+
+/* ---- FDK filtering ----------------------------------------------------------
+ * Replaces Reconstruction.Filtering()/filter_proj/Filter
+ * (Reconstruction_numba.py:190-259): cosine pre-weight, zero-padded ramp
+ * filter along u, times deltaS.  filter_type: 0 ram-lak, 1 shepp-logan,
+ * 2 cosine, 3 hamming, 4 hann.  ctgb_filter_bytes/ctgb_filter_build fill a
+ * host buffer (the filter spectrum and cosine weights, float32) that the
+ * caller copies to device memory once; ctgb_fdk_filter then filters
+ * nrows_total = nviews*nv rows of proj in place. */
+int ctgb_filter_bytes(const ctgb_params *p, size_t *bytes);
+int ctgb_filter_build(const ctgb_params *p, int32_t filter_type, double cutoff, void *host_buf, size_t bytes);
+int ctgb_fdk_filter(const ctgb_params *p, const void *d_filter, float *d_proj, int32_t nviews, void *stream);
+
+/* ---- status ---------------------------------------------------------------- */
+const char *ctgb_last_error(void);
+const char *ctgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTGB_H */

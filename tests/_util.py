@@ -1,0 +1,47 @@
+"""Shared helpers for the tests: golden fixtures and error measures."""
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# Parity bar: float32 results within 1e-4 of the reference / FP64 oracle,
+# measured as max|a-b| / max|b| over the whole projection stack or volume.
+RTOL = 1e-4
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def golden_cases():
+    out = []
+    for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+        d = np.load(f)
+        out.append((os.path.basename(f)[:-4], json.loads(str(d["params"])), str(d["flavour"]), d))
+    return out
+
+
+def golden_ids():
+    return [os.path.basename(f)[:-4] for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))]
+
+
+def load_golden(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return json.loads(str(d["params"])), str(d["flavour"]), d
+
+
+def cone_params(n=24, nviews=16, nu=40, nv=32, du=1.0, dv=1.0, dx=1.0, start=0.0, span=2 * np.pi, **kw):
+    p = {'SourceInit': [0.0, 100.0, 0.0], 'DetectorInit': [0.0, -50.0, 0.0], 'StartAngle': start,
+         'EndAngle': start + span, 'NumberOfDetectorPixels': [nu, nv], 'DetectorPixelSize': [du, dv],
+         'NumberOfViews': nviews, 'ImagePixelSpacing': [dx, dx, dx],
+         'NumberOfImage': [n, n, n] if isinstance(n, int) else list(n),
+         'PhantomCenter': [0.0, 0.0, 0.0], 'RotationOrigin': [0.0, 0.0, 0.0], 'ReconCenter': [0.0, 0.0, 0.0],
+         'Method': 'Distance', 'FilterType': 'hann', 'cutoff': 1.0, 'GPU': 1, 'DetectorShape': 'Flat',
+         'Pitch': 0.0}
+    p.update(kw)
+    return p

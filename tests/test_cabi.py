@@ -1,0 +1,132 @@
+"""libctgb.so on the CPU: it loads, exports every entry point include/ctgb.h
+declares, and its host-side geometry/filter tables agree with the oracle.
+No kernel is launched here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ctreconstruction_gb300 import _lib
+from ctreconstruction_gb300.geometry import ReconstructionParams
+from oracle.oracle import OracleGeometry, ramp_filter
+from _util import cone_params, load_golden
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ctgb.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(ctgb_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = declared_symbols()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+    assert lib.ctgb_version().decode().startswith("ctgb")
+
+
+def _table(params, flavour=None):
+    c = ReconstructionParams.from_dict(params, flavour).to_ctgb()
+    n = ctypes.c_size_t(0)
+    _lib.call("ctgb_table_bytes", ctypes.byref(c), ctypes.byref(n))
+    buf = np.zeros(n.value // 4, dtype=np.float32)
+    _lib.call("ctgb_table_build", ctypes.byref(c), buf.ctypes.data_as(ctypes.c_void_p), n.value)
+    return buf
+
+
+def _header(buf):
+    i = buf.view(np.int32)
+    f = buf
+    h = dict(nx=i[0], ny=i[1], nz=i[2], nu=i[3], nv=i[4], nviews=i[5], curved=i[6], flavour=i[7])
+    names = ["eps_fwd", "eps_bp", "dx", "dy", "dz", "du_bp", "dv_bp", "sad", "sdd", "src0x", "src0y", "src0z",
+             "det0y", "dtheta", "du_fwd", "dv_fwd", "u0_fwd"]
+    for k, nm in enumerate(names):
+        h[nm] = float(f[8 + k])
+    off = buf.view(np.int64)
+    base = (8 + len(names) + 1) // 2   # int64 index after the float block (+pad0)
+    keys = ["off_xplane", "off_yplane", "off_zplane", "off_xpix", "off_ypix", "off_zpix", "off_ki", "off_pp",
+            "off_views", "view_stride"]
+    for k, nm in enumerate(keys):
+        h[nm] = int(off[base + k])
+    return h
+
+
+@pytest.mark.parametrize("name,flavour", [("numba_offcentre", "numba"), ("pycuda_offset", "pycuda"),
+                                          ("numba_helical", "numba"), ("numba_curved", "numba")])
+def test_geometry_table_matches_oracle_geometry(name, flavour):
+    p, fl, _ = load_golden(name)
+    buf = _table(p, fl)
+    h = _header(buf)
+    g = OracleGeometry(p, fl)
+    assert (h["nx"], h["ny"], h["nz"], h["nu"], h["nv"], h["nviews"]) == (g.nx, g.ny, g.nz, g.nu, g.nv, g.nviews)
+    assert h["sad"] == pytest.approx(g.sad, rel=1e-6) and h["sdd"] == pytest.approx(g.sdd, rel=1e-6)
+    assert h["dtheta"] == pytest.approx(g.dtheta, rel=1e-6)
+    C = p['ReconCenter'] if fl == 'pycuda' else p['PhantomCenter']
+    xplane = C[0] + (np.arange(g.nx + 1) - (g.nx - 1) / 2.0) * g.dx - g.dx / 2
+    yplane = C[1] + (np.arange(g.ny + 1) - (g.ny - 1) / 2.0) * -g.dy + g.dy / 2
+    np.testing.assert_allclose(buf[h["off_xplane"]:h["off_xplane"] + g.nx + 1], xplane, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(buf[h["off_yplane"]:h["off_yplane"] + g.ny + 1], yplane, rtol=1e-6, atol=1e-6)
+    # dominant axis per view, restating distance_forward's test (Reconstruction_numba.py:896,966)
+    for v, th in enumerate(g.angles):
+        S = np.array([-g.sad * np.sin(th), g.sad * np.cos(th)])
+        D = np.array([(g.sdd - g.sad) * np.sin(th), -(g.sdd - g.sad) * np.cos(th)])
+        ax, ay = abs(S[0] - D[0]), abs(S[1] - D[1])
+        want = 0 if ax >= ay else 1
+        rec = buf[h["off_views"] + v * h["view_stride"]:]
+        assert int(rec[0]) == want
+
+
+def test_table_rejects_bad_geometry():
+    p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
+    p.nu = 0
+    n = ctypes.c_size_t(0)
+    with pytest.raises(ValueError, match="sizes must be positive"):
+        _lib.call("ctgb_table_bytes", ctypes.byref(p), ctypes.byref(n))
+    p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
+    _lib.call("ctgb_table_bytes", ctypes.byref(p), ctypes.byref(n))
+    small = np.zeros(8, dtype=np.float32)
+    with pytest.raises(ValueError, match="too small"):
+        _lib.call("ctgb_table_build", ctypes.byref(p), small.ctypes.data_as(ctypes.c_void_p), small.nbytes)
+
+
+def test_null_device_pointers_are_rejected_without_a_launch():
+    p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
+    with pytest.raises(ValueError, match="NULL"):
+        _lib.call("ctgb_forward", ctypes.byref(p), None, None, None, None, 0, 1, None)
+    with pytest.raises(ValueError, match="view range"):
+        _lib.call("ctgb_backproject_fdk", ctypes.byref(p), ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), 10, 100, 1.0, 0, None)
+
+
+@pytest.mark.parametrize("ft,cut", [("ram-lak", 1.0), ("shepp-logan", 0.3), ("cosine", 1.0), ("hamming", 1.0),
+                                    ("hann", 0.5)])
+def test_filter_table_matches_oracle_spectrum(ft, cut):
+    params = cone_params(nu=40, nv=8, du=0.7)
+    c = ReconstructionParams.from_dict(params).to_ctgb()
+    n = ctypes.c_size_t(0)
+    _lib.call("ctgb_filter_bytes", ctypes.byref(c), ctypes.byref(n))
+    buf = np.zeros(n.value // 4, dtype=np.float32)
+    _lib.call("ctgb_filter_build", ctypes.byref(c), _lib.FILTER_TYPES[ft], cut, buf.ctypes.data_as(ctypes.c_void_p),
+              n.value)
+    i = buf.view(np.int32)
+    zpl = int(i[0])
+    assert zpl == int(2 ** np.ceil(np.log2(2.0 * (40 - 1))))
+    off_h = int(buf.view(np.int64)[4])
+    R, D = 100.0, 50.0
+    tau = 0.7 * R / (R + D)
+    want = np.fft.ifftshift(ramp_filter(zpl + 1, tau, ft, cut)) * tau / zpl
+    np.testing.assert_allclose(buf[off_h:off_h + zpl], want, rtol=2e-6, atol=1e-7 * np.abs(want).max())
+
+
+def test_product_never_imports_the_oracle():
+    pkg = os.path.join(os.path.dirname(HEADER), "..", "ctreconstruction_gb300")
+    for root, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
+                text = open(os.path.join(root, f)).read()
+                assert "import oracle" not in text and "from oracle" not in text, f

@@ -1,0 +1,147 @@
+"""Parity of the CUDA path (through the C ABI, via Projector/Reconstruction)
+with the reference's golden vectors and with the FP64 oracle.
+
+Bar: max|gpu - ref| / max|ref| <= 1e-4 for every projection stack, volume and
+filtered stack (float32 arithmetic on both sides)."""
+import numpy as np
+import pytest
+import torch
+
+from ctreconstruction_gb300 import Projector, Reconstruction
+from oracle.oracle import OracleGeometry
+from _util import RTOL, cone_params, golden_ids, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _t(a, dev):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+
+
+@pytest.mark.parametrize("name", golden_ids())
+def test_golden_forward_backward(cuda, name):
+    p, flavour, d = load_golden(name)
+    P = Projector(p, flavour=flavour)
+    if "forward" in d.files:
+        out = P.forward(_t(d["image"], cuda)).cpu().numpy()
+        assert rel_err(out, d["forward"]) < RTOL
+    if "backward" in d.files:
+        out = P.backproject_fdk(_t(d["proj"], cuda)).cpu().numpy()
+        assert rel_err(out, d["backward"]) < RTOL
+
+
+@pytest.mark.parametrize("name", [n for n in golden_ids() if n in ("numba_basic", "numba_fan", "pycuda_basic",
+                                                                     "pycuda_offset")])
+def test_golden_filtering(cuda, name):
+    p, flavour, d = load_golden(name)
+    P = Projector(p, flavour=flavour)
+    keys = [k for k in d.files if k.startswith("filter_")]
+    assert keys
+    for k in keys:
+        _, ft, co = k.split("_")
+        q = _t(d["proj"], cuda)
+        P.filter(q, ft, float(co))
+        assert rel_err(q.cpu().numpy(), d[k]) < RTOL, k
+
+
+def test_reconstruction_class_roundtrip(cuda):
+    p, flavour, d = load_golden("numba_basic")
+    R = Reconstruction(p, flavour=flavour)
+    R.image = d["image"].copy()
+    R.forward()
+    assert isinstance(R.proj, np.ndarray) and rel_err(R.proj, d["forward"]) < RTOL
+    R.proj = d["proj"].copy()
+    R.Filtering()
+    assert rel_err(R.proj, d["filter_hann_1"]) < RTOL
+    R.proj = _t(d["proj"], cuda)
+    R.backward()
+    assert isinstance(R.image, torch.Tensor) and rel_err(R.image.cpu().numpy(), d["backward"]) < RTOL
+
+
+GEOMS = {
+    "cone_y_and_x_views": cone_params(n=(20, 18, 16), nviews=24, nu=36, nv=28, dx=0.9),
+    "offcentre_short_scan": cone_params(n=(17, 21, 13), nviews=13, nu=30, nv=26, start=0.4, span=np.pi + 0.6,
+                                        PhantomCenter=[1.1, -0.7, 0.4], ReconCenter=[-0.6, 0.8, -0.3]),
+    "fine_detector": cone_params(n=16, nviews=10, nu=64, nv=48, du=0.35, dv=0.4),
+    "coarse_detector": cone_params(n=24, nviews=10, nu=16, nv=12, du=2.7, dv=2.9),
+    "helical": cone_params(n=16, nviews=20, nu=32, nv=16, Pitch=0.7, start=0.0, span=4 * np.pi),
+    "curved": cone_params(n=18, nviews=12, nu=36, nv=24, DetectorShape='Curved'),
+    "pycuda_offset": dict(cone_params(n=(19, 15, 11), nviews=11, nu=33, nv=21, ReconCenter=[0.3, -0.2, 0.5]),
+                          DetectorOffset=[0.6, -0.45]),
+}
+
+
+@pytest.mark.parametrize("gname", sorted(GEOMS))
+def test_against_fp64_oracle(cuda, gname):
+    p = GEOMS[gname]
+    flavour = "pycuda" if "DetectorOffset" in p else "numba"
+    g = OracleGeometry(p, flavour)
+    P = Projector(p, flavour=flavour)
+    rng = np.random.default_rng(abs(hash(gname)) % 2 ** 32)
+    x = rng.random((g.nz, g.ny, g.nx), dtype=np.float32)
+    y = rng.random((g.nviews, g.nv, g.nu), dtype=np.float32)
+    assert rel_err(P.forward(_t(x, cuda)).cpu().numpy(), g.forward(x)) < RTOL
+    assert rel_err(P.backproject_fdk(_t(y, cuda)).cpu().numpy(), g.backward_fdk(y)) < RTOL
+    assert rel_err(P.backproject_matched(_t(y, cuda)).cpu().numpy(), g.backward_matched(y)) < RTOL
+
+
+@pytest.mark.parametrize("gname", ["cone_y_and_x_views", "curved", "helical"])
+def test_matched_backprojector_is_adjoint(cuda, gname):
+    """Dot-product test <A x, y> = <x, A^T y> to 1e-5 relative."""
+    p = GEOMS[gname]
+    P = Projector(p)
+    gen = torch.Generator(device=cuda).manual_seed(3)
+    x = torch.randn(P.volume_shape, device=cuda, generator=gen)
+    y = torch.randn(P.proj_shape(), device=cuda, generator=gen)
+    lhs = torch.sum(P.forward(x).double() * y.double()).item()
+    rhs = torch.sum(x.double() * P.backproject_matched(y).double()).item()
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+
+
+def test_forward_without_transposed_copy_matches(cuda):
+    p = GEOMS["cone_y_and_x_views"]
+    P = Projector(p)
+    x = torch.rand(P.volume_shape, device=cuda)
+    a = P.forward(x)
+    b = torch.empty_like(a)
+    from ctreconstruction_gb300 import _lib
+    import ctypes
+    _lib.call("ctgb_forward", ctypes.byref(P.c), ctypes.c_void_p(P.table.data_ptr()), ctypes.c_void_p(x.data_ptr()),
+              None, ctypes.c_void_p(b.data_ptr()), 0, P.params.NumberOfViews,
+              ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+
+
+def test_view_ranges_and_accumulate(cuda):
+    p = GEOMS["cone_y_and_x_views"]
+    P = Projector(p)
+    x = torch.rand(P.volume_shape, device=cuda)
+    full = P.forward(x)
+    part = torch.cat([P.forward(x, view0=0, nviews=7), P.forward(x, view0=7, nviews=17)])
+    assert torch.equal(full, part)
+    y = torch.rand(P.proj_shape(), device=cuda)
+    whole = P.backproject_fdk(y)
+    acc = P.backproject_fdk(y[:9].contiguous(), view0=0, nviews=9)
+    P.backproject_fdk(y[9:].contiguous(), out=acc, view0=9, nviews=15, accumulate=True)
+    assert rel_err(acc.cpu().numpy(), whole.cpu().numpy()) < 1e-6
+
+
+def test_deterministic(cuda):
+    p = GEOMS["offcentre_short_scan"]
+    P = Projector(p)
+    x = torch.rand(P.volume_shape, device=cuda)
+    y = torch.rand(P.proj_shape(), device=cuda)
+    assert torch.equal(P.forward(x), P.forward(x))
+    assert torch.equal(P.backproject_fdk(y), P.backproject_fdk(y))
+    assert torch.equal(P.backproject_matched(y), P.backproject_matched(y))
+
+
+def test_bad_inputs_raise(cuda):
+    P = Projector(GEOMS["curved"])
+    with pytest.raises(ValueError):
+        P.forward(torch.rand(P.volume_shape))            # CPU tensor
+    with pytest.raises(ValueError):
+        P.forward(torch.rand(P.volume_shape, device=cuda, dtype=torch.float64))
+    with pytest.raises(ValueError):
+        P.forward(torch.rand((3, 3, 3), device=cuda))
