@@ -40,6 +40,7 @@ SIGNATURES = {
     "ctgb_filter_bytes": [_P, ctypes.POINTER(_sz)],
     "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],
     "ctgb_fdk_filter": [_P, _vp, _vp, _i32, _vp],
+    "ctgb_device_status": [ctypes.POINTER(_i32), _i32],
 }
 STRING_FUNCS = ("ctgb_last_error", "ctgb_version")
 

@@ -29,88 +29,187 @@
 
 #include "dd_common.cuh"
 #include "status.h"
+#include "tma.cuh"
 
 namespace ctgb {
 
-constexpr int kBpTileX = 32, kBpTileY = 4, kZc = 8;
+constexpr int kBpTileX = 32, kBpTileY = 4;
+
+// ---------------------------------------------------------------------------
+// FDK-weighted DD backprojection, table form (the default path).
+//
+// Per (voxel column, view) the u footprint is z-independent, so the column
+// first builds G(m) = sum_l Q[m][l] * w_u(l) for the detector rows its kBpZ
+// voxels can reach, with running sums C(m) = sum_{m' < m} G(m'), in shared
+// memory.  Each voxel's v footprint [lo, hi] (detector-row units) then costs
+// two lookups: integral = (C + G*frac)(hi) - (C + G*frac)(lo), divided by the
+// footprint width — the reference's weight_calculator1 sum written as an
+// integral of a piecewise-constant function.  With the source outside the
+// volume every corner depth 1/(S_y - y_c) is positive, so the min/max over the
+// 8 corner slopes reduces to one product per z end.  Columns whose footprint
+// falls outside these assumptions (more than 4 u cells, more than kBpRows rows,
+// a corner behind the source) take the direct per-cell loop.
+constexpr int kBpZ = 16, kBpRows = 24, kBpTX = 32, kBpTY = 4;
+
+__device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
+
+// v footprint (detector-row units) of the voxel with centre height zc: with
+// every corner depth factor i = 1/(S_y - y_c) in [imin, imax], imin > 0, the
+// min/max of (S_z - z_end) * i over the 8 corners are n_small * (imax if
+// n_small < 0 else imin) and n_big * (imax if n_big > 0 else imin).
+__device__ __forceinline__ void v_footprint(float zc, float hz, float Sz, float imin, float imax, float Mv, float Av,
+                                            float *lo, float *hi) {
+    const float n1 = Sz - (zc - hz), n2 = Sz - (zc + hz);
+    const float ns = fminf(n1, n2), nb = fmaxf(n1, n2);
+    const float a = ns * ((ns < 0.0f) ? imax : imin);
+    const float b = nb * ((nb > 0.0f) ? imax : imin);
+    const float va = fmaf(a, Mv, Av), vb = fmaf(b, Mv, Av);
+    *lo = fminf(va, vb);
+    *hi = fmaxf(va, vb);
+}
 
 template <bool CURVED>
-__global__ void __launch_bounds__(kBpTileX * kBpTileY)
-bp_fdk_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
-              int nviews, float scale, int accumulate) {
+__global__ void __launch_bounds__(kBpTX * kBpTY, 6)
+bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
+                    int nviews, float scale, int accumulate) {
+    __shared__ float2 gtab[kBpRows][kBpTX * kBpTY];
     const TableHeader &h = header(T);
-    const int ix = blockIdx.x * kBpTileX + threadIdx.x;
-    const int iy = blockIdx.y * kBpTileY + threadIdx.y;
-    const int z0 = blockIdx.z * kZc;
-    if (ix >= h.nx || iy >= h.ny) return;
-    const float *__restrict__ xpix = T + h.off_xpix;
-    const float *__restrict__ ypix = T + h.off_ypix;
-    const float *__restrict__ zpix = T + h.off_zpix;
+    const int tid = threadIdx.y * kBpTX + threadIdx.x;
+    const int ix = blockIdx.x * kBpTX + threadIdx.x;
+    const int iy = blockIdx.y * kBpTY + threadIdx.y;
+    const int z0 = blockIdx.z * kBpZ;
+    const bool live = ix < h.nx && iy < h.ny;
+    const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
     const float *__restrict__ ki = T + h.off_ki;
     const float *__restrict__ pp = T + h.off_pp;
-    const int nu = h.nu, nv = h.nv;
-    const float xx = xpix[ix], yy = ypix[iy];
-    const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f;
+    const int nu = h.nu, nv = h.nv, nz = h.nz;
+    const int zlast = min(z0 + kBpZ, nz) - 1 - z0;            // last voxel of the chunk (relative)
+    const float xx = T[h.off_xpix + ixc], yy = T[h.off_ypix + iyc];
+    const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f, dzs = h.dz;
     const float du = h.du_bp, dv = h.dv_bp, inv_du = 1.0f / du, inv_dv = 1.0f / dv;
-    const float abs_du = fabsf(du), abs_dv = fabsf(dv);
     const float ki0 = ki[0], pp0 = pp[0];
     const float Sx = h.src0x, Sy = h.src0y, Dy = h.det0y, R = h.sad;
     const float eps = h.eps_bp;
-    float zz[kZc];
-    float acc[kZc];
+    const float zfirst = T[h.off_zpix + min(z0, nz - 1)];
+    float acc[kBpZ];
 #pragma unroll
-    for (int j = 0; j < kZc; ++j) {
-        zz[j] = (z0 + j < h.nz) ? zpix[z0 + j] : 0.0f;
-        acc[j] = 0.0f;
-    }
+    for (int j = 0; j < kBpZ; ++j) acc[j] = 0.0f;
+
     for (int vi = 0; vi < nviews; ++vi) {
         const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
         const float cs = V[VF_COS], sn = V[VF_SIN], Sz = V[VF_BPSZ];
+        const float *__restrict__ Q = proj + (long long)vi * nu * nv;
         const float yc = yy * cs - xx * sn;
         float umin = INFINITY, umax = -INFINITY, imin = INFINITY, imax = -INFINITY;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const float cx = xx + ((q & 1) ? hx : -hx), cy = yy + ((q & 2) ? hy : -hy);
             const float xr = cx * cs + cy * sn, yr = cy * cs - cx * sn;
-            const float su = (Sx - xr) / (Sy - yr);
-            const float inv = 1.0f / (Sy - yr);
+            const float inv = fast_rcp(Sy - yr);
+            const float su = (Sx - xr) * inv;
             umin = fminf(umin, su); umax = fmaxf(umax, su);
             imin = fminf(imin, inv); imax = fmaxf(imax, inv);
         }
         float cu1, cu2;
         if (CURVED) { cu1 = -atanf(umin); cu2 = -atanf(umax); }
-        else { cu1 = umin * Dy + (Sx - umin * Sy); cu2 = umax * Dy + (Sx - umax * Sy); }
-        const Span us = make_span(cu1, cu2, ki0, inv_du);
-        const int l0 = max(us.s, 0), l1 = min(us.e, nu - 1);
-        const float W = scale * (R * R) / ((R - yc) * (R - yc));
-        const float *__restrict__ Q = proj + (long long)vi * nu * nv;
+        else { cu1 = fmaf(umin, Dy - Sy, Sx); cu2 = fmaf(umax, Dy - Sy, Sx); }
+        const float ua = (cu1 - ki0) * inv_du, ub = (cu2 - ki0) * inv_du;
+        const float ulo = fminf(ua, ub), uhi = fmaxf(ua, ub);
+        float fl0;
+        const int l0 = floor_split(ulo, &fl0);
+        const float uw = uhi - ulo;
+        const float Rd = R - yc;
+        const float W = scale * (R * R) * fast_rcp(Rd * Rd);
+        const float Mv = (Dy - Sy) * inv_dv, Av = (Sz - pp0) * inv_dv;
+        // Rows the chunk's footprints reach: footprints move monotonically with z,
+        // so the first and last voxels bound them (one row of margin each side).
+        float vlo0, vhi0, vloN, vhiN;
+        v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &vlo0, &vhi0);
+        v_footprint(zfirst + (float)zlast * dzs, hz, Sz, imin, imax, Mv, Av, &vloN, &vhiN);
+        const int mlo = (int)floorf(fminf(vlo0, vloN)) - 1;
+        const int mhi = (int)floorf(fmaxf(vhi0, vhiN)) + 1;
+        const bool simple = live && imin > 0.0f && (uhi - fl0) <= 4.0f && (mhi - mlo + 1 <= kBpRows);
+        if (simple) {
+            float ov[4];
 #pragma unroll
-        for (int j = 0; j < kZc; ++j) {
-            const float nlo = Sz - (zz[j] - hz), nhi = Sz - (zz[j] + hz);
-            const float a0 = nlo * imin, a1 = nlo * imax, a2 = nhi * imin, a3 = nhi * imax;
-            const float vmin = fminf(fminf(a0, a1), fminf(a2, a3));
-            const float vmax = fmaxf(fmaxf(a0, a1), fmaxf(a2, a3));
-            const float cv1 = vmin * Dy + (Sz - vmin * Sy), cv2 = vmax * Dy + (Sz - vmax * Sy);
-            const Span vs = make_span(cv1, cv2, pp0, inv_dv);
-            const int k0 = max(vs.s, 0), k1 = min(vs.e, nv - 1);
-            float sum = 0.0f;
-            for (int k = k0; k <= k1; ++k) {
-                const float w1 = span_weight<true>(vs, k, pp[k], pp[k + 1], abs_dv, eps);
-                const float *__restrict__ qrow = Q + (long long)k * nu;
-                float part = 0.0f;
-                for (int l = l0; l <= l1; ++l) {
-                    const float w2 = span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
-                    part += __ldg(qrow + l) * w2;
+            for (int t = 0; t < 4; ++t)
+                ov[t] = fmaxf(0.0f, fminf(fl0 + (float)(t + 1), uhi) - fmaxf(fl0 + (float)t, ulo));
+            float wscale = W;
+            if (uw > 1e-6f) wscale *= fast_rcp(uw);
+            else { ov[0] = 1.0f; ov[1] = ov[2] = ov[3] = 0.0f; }
+            int ntl = 1;
+#pragma unroll
+            for (int t = 1; t < 4; ++t) ntl = (ov[t] > 0.0f) ? t + 1 : ntl;
+            // G(m) with running sums C(m) for rows mlo..mhi.
+            const bool inner = l0 >= 0 && l0 + 3 < nu;
+            float run = 0.0f;
+            const int nrows = mhi - mlo + 1;
+            for (int i = 0; i < nrows; ++i) {
+                const int m = mlo + i;
+                float g = 0.0f;
+                if (m >= 0 && m < nv) {
+                    const float *__restrict__ row = Q + (long long)m * nu + l0;
+                    if (inner) {
+                        g = __ldg(row) * ov[0] + __ldg(row + 1) * ov[1];
+                        if (ntl > 2) g += __ldg(row + 2) * ov[2];
+                        if (ntl > 3) g += __ldg(row + 3) * ov[3];
+                    } else {
+#pragma unroll
+                        for (int t = 0; t < 4; ++t)
+                            if (t < ntl && l0 + t >= 0 && l0 + t < nu) g += __ldg(row + t) * ov[t];
+                    }
                 }
-                sum += part * w1;
+                gtab[i][tid] = make_float2(run, g);
+                run += g;
             }
-            acc[j] += sum * W;
+#pragma unroll
+            for (int j = 0; j < kBpZ; ++j) {
+                float vlo, vhi, fa, fb;
+                v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &vlo, &vhi);
+                const int ma = min(max(floor_split(vlo, &fa) - mlo, 0), kBpRows - 1);
+                const int mb = min(max(floor_split(vhi, &fb) - mlo, 0), kBpRows - 1);
+                const float2 A = gtab[ma][tid];
+                const float2 B = gtab[mb][tid];
+                const float width = vhi - vlo;
+                const float integ = (B.x + B.y * (vhi - fb)) - (A.x + A.y * (vlo - fa));
+                const float val = (width > 1e-6f) ? integ * fast_rcp(width) : A.y;
+                acc[j] = fmaf(val, wscale, acc[j]);
+            }
+        } else if (live) {
+            // Direct per-cell loop (reference weight calculators).
+            const Span us = make_span(cu1, cu2, ki0, inv_du);
+            const int c0 = max(us.s, 0), c1 = min(us.e, nu - 1);
+            const float abs_du = fabsf(du), abs_dv = fabsf(dv);
+            for (int j = 0; j <= zlast; ++j) {
+                const float zc = zfirst + (float)j * dzs;
+                const float nlo = Sz - (zc - hz), nhi = Sz - (zc + hz);
+                const float a0 = nlo * imin, a1 = nlo * imax, a2 = nhi * imin, a3 = nhi * imax;
+                const float vmn = fminf(fminf(a0, a1), fminf(a2, a3));
+                const float vmx = fmaxf(fmaxf(a0, a1), fmaxf(a2, a3));
+                const float cv1 = fmaf(vmn, Dy - Sy, Sz), cv2 = fmaf(vmx, Dy - Sy, Sz);
+                const Span vs = make_span(cv1, cv2, pp0, inv_dv);
+                const int k0 = max(vs.s, 0), k1 = min(vs.e, nv - 1);
+                float sum = 0.0f;
+                for (int k = k0; k <= k1; ++k) {
+                    const float w1 = span_weight<true>(vs, k, pp[k], pp[k + 1], abs_dv, eps);
+                    const float *__restrict__ qrow = Q + (long long)k * nu;
+                    float part = 0.0f;
+                    for (int l = c0; l <= c1; ++l)
+                        part += __ldg(qrow + l) * span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
+                    sum += part * w1;
+                }
+                gtab[j][tid] = make_float2(sum * W, 0.0f);
+            }
+#pragma unroll
+            for (int j = 0; j < kBpZ; ++j)
+                if (j <= zlast) acc[j] += gtab[j][tid].x;
         }
     }
+    if (!live) return;
 #pragma unroll
-    for (int j = 0; j < kZc; ++j) {
+    for (int j = 0; j < kBpZ; ++j) {
         const int iz = z0 + j;
-        if (iz < h.nz) {
+        if (iz < nz) {
             float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
             *dst = accumulate ? *dst + acc[j] : acc[j];
         }
@@ -176,6 +275,140 @@ __device__ float matched_voxel_view(const TableHeader &h, const float *__restric
     return acc;
 }
 
+// Matched backprojection, sweep form, for views whose dominant axis is x or y:
+// the exact transpose of dd_forward_tma_kernel's arithmetic.  A voxel column
+// (ix, iy) lies in one slice s of such a view at one transverse index k, so
+// the detector columns whose footprint overlaps it, and their overlaps
+// ov_x, are z-independent.  For each such column the rows' z intervals
+// [z'_r, z'_{r+1}] tile the z axis; spreading v_r = y[r][c] * K_rc * ov_x * g
+// uniformly over row r's interval and integrating over each voxel [l, l+1]
+// gives voxel l = R(l+1) - R(l) with R the running integral, evaluated by a
+// merge of row boundaries and voxel boundaries.
+constexpr int kMZ = 16;
+
+__global__ void __launch_bounds__(kBpTileX * kBpTileY, 6)
+bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol,
+                        int view0, int nviews, float scale, int accumulate) {
+    const TableHeader &h = header(T);
+    const int ix = blockIdx.x * kBpTileX + threadIdx.x;
+    const int iy = blockIdx.y * kBpTileY + threadIdx.y;
+    const int l0 = blockIdx.z * kMZ;
+    if (ix >= h.nx || iy >= h.ny) return;
+    const int nu = h.nu, nv = h.nv, nz = h.nz;
+    const ViewOffsets vo = view_offsets(nu, nv);
+    const float *__restrict__ pzp = T + h.off_zplane;
+    const float inv_dz = 1.0f / h.dz;
+    float acc[kMZ];
+#pragma unroll
+    for (int j = 0; j < kMZ; ++j) acc[j] = 0.0f;
+
+    for (int vi = 0; vi < nviews; ++vi) {
+        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+        const float *__restrict__ Q = proj + (long long)vi * nu * nv;
+        const int axis = (int)V[VF_AXIS];
+        if (axis == 2) {
+#pragma unroll
+            for (int j = 0; j < kMZ; ++j)
+                if (l0 + j < nz) acc[j] += matched_voxel_view<2>(h, T, V, vo, Q, ix, iy, l0 + j);
+            continue;
+        }
+        const bool xd = axis == 0;
+        const int s = xd ? ix : iy, k = xd ? iy : ix;
+        const float *__restrict__ pa = T + (xd ? h.off_xplane : h.off_yplane);
+        const float *__restrict__ pb = T + (xd ? h.off_yplane : h.off_xplane);
+        const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
+        const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
+        const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
+        const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
+        const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
+        const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
+        const float *__restrict__ Bzr = V + vo.bz;
+        const float *__restrict__ Pzr = V + vo.pz;
+        const float inv_db = 1.0f / db;
+        const float Cb = (Sb - pb[0]) * inv_db;
+        const float A = (Sz - pzp[0]) * inv_dz;
+        const float q = pa[s] + 0.5f * da - Sa;
+        const float g = 1.0f / (q * q);
+        // Candidate columns: project the voxel's b1 edges on the slice centre plane.
+        float cmin = INFINITY, cmax = -INFINITY;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float bw = pb[k + e];
+            const float ddx = (xd ? pa[s] + 0.5f * da : bw) - V[VF_SX];
+            const float ddy = (xd ? bw : pa[s] + 0.5f * da) - V[VF_SY];
+            const float aa = ddx * V[VF_EUX] + ddy * V[VF_EUY], bb = ddx * V[VF_EWX] + ddy * V[VF_EWY];
+            const float u = h.curved ? atan2f(aa, bb) : h.sdd * aa / bb;
+            const float cu = (u - h.u0_fwd) / h.du_fwd;
+            cmin = fminf(cmin, cu); cmax = fmaxf(cmax, cu);
+        }
+        const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
+        const float kf = (float)k;
+        for (int c = cA; c <= cB; ++c) {
+            const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
+            const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
+            const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
+            const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
+            const float ovx = fminf(kf + 1.0f, hi) - fmaxf(kf, lo);
+            if (!(ovx > 0.0f)) continue;
+            const float invD = 1.0f / (Sa - Pa[c]);
+            const float t1 = (Sb - Pb[c]) * invD;
+            const float tau = q * invD;
+            const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
+            const float vscale = ovx * g * base;
+            // First row whose lower boundary lies above voxel boundary l0.
+            int r = 0;
+            {
+                const float B0 = (Sz - Bzr[0]) * inv_dz, B1 = (Sz - Bzr[1]) * inv_dz;
+                const float est = (((float)l0 - A) / tau - B0) / (B1 - B0);
+                r = min(max((int)floorf(est) - 1, 0), nv);
+            }
+            // Row r spans [zr, zr1]; C = running integral up to zr.
+            float Bcur = (Sz - Bzr[r]) * inv_dz;
+            float zr = fmaf(Bcur, tau, A);
+            float C = 0.0f, vr = 0.0f, zr1 = zr, Bnext = Bcur;
+            bool have_row = false;
+            auto load_row = [&]() {
+                if (r < nv) {
+                    Bnext = (Sz - Bzr[r + 1]) * inv_dz;
+                    zr1 = fmaf(Bnext, tau, A);
+                    const float t2 = (Sz - Pzr[r]) * invD;
+                    const float K = sqrtf(1.0f + t2 * t2) / fabsf(Bnext - Bcur);
+                    vr = __ldg(Q + (long long)r * nu + c) * K * vscale;
+                    have_row = true;
+                } else {
+                    have_row = false;
+                    vr = 0.0f;
+                }
+            };
+            load_row();
+            float Rprev = 0.0f;
+#pragma unroll
+            for (int j = 0; j <= kMZ; ++j) {
+                const float lb = (float)(l0 + j);
+                // Advance past rows that end at or below this voxel boundary.
+                while (have_row && zr1 <= lb) {
+                    C += vr * (zr1 - zr);
+                    zr = zr1;
+                    Bcur = Bnext;
+                    ++r;
+                    load_row();
+                }
+                const float Rb = C + ((have_row && lb > zr) ? vr * (lb - zr) : 0.0f);
+                if (j > 0) acc[j - 1] += Rb - Rprev;
+                Rprev = Rb;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kMZ; ++j) {
+        const int iz = l0 + j;
+        if (iz < nz) {
+            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
+            *dst = accumulate ? *dst + scale * acc[j] : scale * acc[j];
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBpTileX * kBpTileY)
 bp_matched_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
                   int nviews, float scale, int accumulate) {
@@ -216,14 +449,23 @@ extern "C" int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, c
     clear_error();
     int st = bp_args(p, d_table, d_proj, d_vol, view0, nviews, "ctgb_backproject_fdk");
     if (st) return st;
-    dim3 block(kBpTileX, kBpTileY);
-    dim3 grid((p->nx + kBpTileX - 1) / kBpTileX, (p->ny + kBpTileY - 1) / kBpTileY, (p->nz + kZc - 1) / kZc);
     const float *T = static_cast<const float *>(d_table);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (p->curved) bp_fdk_kernel<true><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
-    else bp_fdk_kernel<false><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
+    if (nviews == 0) {
+        if (!accumulate) {
+            cudaError_t e = cudaMemsetAsync(d_vol, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nz, s);
+            if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
+        return CTGB_OK;
+    }
+    dim3 block(kBpTX, kBpTY);
+    dim3 grid((p->nx + kBpTX - 1) / kBpTX, (p->ny + kBpTY - 1) / kBpTY, (p->nz + kBpZ - 1) / kBpZ);
+    if (p->curved)
+        bp_fdk_table_kernel<true><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
+    else
+        bp_fdk_table_kernel<false><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_kernel: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_table_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
 }
 
@@ -233,10 +475,9 @@ extern "C" int ctgb_backproject_matched(const ctgb_params *p, const void *d_tabl
     clear_error();
     int st = bp_args(p, d_table, d_proj, d_vol, view0, nviews, "ctgb_backproject_matched");
     if (st) return st;
-    if (p->nz > 65535) return set_error(CTGB_ERR_SIZE, "ctgb_backproject_matched: nz above 65535");
     dim3 block(kBpTileX, kBpTileY);
-    dim3 grid((p->nx + kBpTileX - 1) / kBpTileX, (p->ny + kBpTileY - 1) / kBpTileY, p->nz);
-    bp_matched_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
+    dim3 grid((p->nx + kBpTileX - 1) / kBpTileX, (p->ny + kBpTileY - 1) / kBpTileY, (p->nz + kMZ - 1) / kMZ);
+    bp_matched_sweep_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const float *>(d_table), d_proj, d_vol, view0, nviews, scale, accumulate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_kernel: %s", cudaGetErrorString(e));

@@ -18,8 +18,13 @@
 // four floor-conversions and the (usually 2x2) weighted gather per slice.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "dd_common.cuh"
 #include "status.h"
+#include "tma.cuh"
 
 namespace ctgb {
 
@@ -110,6 +115,265 @@ __global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restr
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// TMA forward projector for views whose dominant axis is x (XD) or y.
+//
+// One warp = one CTA owns a tile of kTU = 32 detector columns (one per lane) x
+// kTR = 16 rows of one view.  It walks the slices along the dominant axis; for
+// each slice the tile's footprint on the slice (a window of the volume, at
+// most kPX x kPZ voxels) is brought into shared memory by TMA boxes of
+// 64 x 1 x 8 voxels (double-buffered, one mbarrier per buffer; the next
+// slice's boxes are in flight while this slice is computed).  Out-of-volume
+// voxels arrive as zeros (TMA OOB fill), which is the reference's bounds test.
+//
+// Maths per pixel and slice (same result as the weight-calculator loop):
+//   * the column footprint [x1', x2'] and row boundaries z'_j are linear in
+//     q = pc - S_a (every boundary ray passes through the source), so both
+//     footprint widths are |q| times a per-pixel constant and the reference's
+//     two weight denominators become K_pixel / q^2 — one factor per slice;
+//   * h(m) = sum_k P[m][k] * overlap_x(k) for the lane's column (2-4 taps,
+//     overlaps in voxel units), and the row integral over [z'_j, z'_j+1] is
+//     sum of whole cells + e(z'_j+1) - e(z'_j) with e(z) = h(floor z) * frac(z),
+//     so consecutive rows share their boundary term.
+// Slices whose window exceeds the patch, or whose footprint is wider than 4
+// voxels, are integrated cell by cell from global memory (compact, rare path).
+constexpr int kTU = 32, kTR = 16, kBoxX = 64, kBoxZ = 8, kPZ = 32, kPX = kBoxX;
+
+struct FwdTmaSmem {
+    float buf[2][kPZ][kPX];
+    float spill[kTR][kTU];      // per-slice row values of the fallback path
+    uint64_t bar[2];
+};
+
+struct TileWindow {
+    int kb, lb, nbz;     // patch origin (kb multiple of 4) and number of 8-row boxes
+    bool active, fits;
+};
+
+// h(m): the lane's column footprint applied to patch row m.
+struct PatchCells {
+    const float *base;   // &patch[0][k0 - kb]
+    int lb, nt;
+    float ov0, ov1, ov2, ov3;
+    __device__ __forceinline__ float operator()(int m) const {
+        const float *p = base + (m - lb) * kPX;
+        float v = p[0] * ov0 + p[1] * ov1;
+        if (nt > 2) v += p[2] * ov2;
+        if (nt > 3) v += p[3] * ov3;
+        return v;
+    }
+};
+
+// Integrate h over consecutive row boundaries of one chain of N rows.
+template <int N>
+__device__ __forceinline__ void sweep_rows(const PatchCells &H, const float *Bj, float A, float tau, float g,
+                                           float *acc) {
+    float f0;
+    const float z0 = fmaf(Bj[0], tau, A);
+    int m0 = floor_split(z0, &f0);
+    float h0 = H(m0);
+    float e0 = h0 * (z0 - f0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        float f1;
+        const float z1 = fmaf(Bj[j + 1], tau, A);
+        const int m1 = floor_split(z1, &f1);
+        const float h1 = H(m1);
+        const float e1 = h1 * (z1 - f1);
+        float whole = (m1 > m0) ? h0 : 0.0f;
+        if (__any_sync(0xffffffffu, m1 > m0 + 1)) {
+            for (int m = m0 + 1; m < m1; ++m) whole += H(m);
+        }
+        acc[j] = fmaf(whole + e1 - e0, g, acc[j]);
+        m0 = m1; h0 = h1; e0 = e1;
+    }
+}
+
+template <bool XD, bool TMA>
+__global__ void __launch_bounds__(32)
+dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
+                      const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0, int vbase,
+                      int ntu, int *status) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    FwdTmaSmem &sm = *reinterpret_cast<FwdTmaSmem *>(smraw);
+    const TableHeader &h = header(T);
+    const int lane = threadIdx.x;
+    const int vi = vbase + blockIdx.x;            // view index relative to view0
+    const int tu = blockIdx.y % ntu, tv = blockIdx.y / ntu;
+    const int c0 = tu * kTU, r0 = tv * kTR;
+    const int nu = h.nu, nv = h.nv;
+    const ViewOffsets vo = view_offsets(nu, nv);
+    const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+    const int c = c0 + lane;
+
+    const float *__restrict__ pa = T + (XD ? h.off_xplane : h.off_yplane);
+    const float *__restrict__ pb = T + (XD ? h.off_yplane : h.off_xplane);
+    const float *__restrict__ pzp = T + h.off_zplane;
+    const float da = XD ? h.dx : h.dy, db = XD ? h.dy : h.dx, dz = h.dz;
+    const int nA = XD ? h.nx : h.ny, nB = XD ? h.ny : h.nx, nZ = h.nz;
+    // Strides of src in (slice, transverse, z): [z][x][y] copy or [z][y][x] volume.
+    const long long st_s = XD ? (st_k == 1 ? (long long)h.ny : 1LL) : (long long)h.nx;
+    const long long st_l = (long long)h.nx * h.ny;
+    const float Sa = XD ? V[VF_SX] : V[VF_SY], Sb = XD ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
+    const float *__restrict__ Ba = V + (XD ? vo.bx : vo.by);
+    const float *__restrict__ Bb = V + (XD ? vo.by : vo.bx);
+    const float *__restrict__ Pa = V + (XD ? vo.px : vo.py);
+    const float *__restrict__ Pb = V + (XD ? vo.py : vo.px);
+    const float *__restrict__ Bzr = V + vo.bz;
+    const float *__restrict__ Pzr = V + vo.pz;
+
+    // Column constants (lanes beyond nu use the last column and do not write).
+    const int cc = min(c, nu - 1);
+    const float inv_db = 1.0f / db, inv_dz = 1.0f / dz;
+    const float Eb0 = (Sb - Bb[cc]) / (Sa - Ba[cc]) * inv_db;
+    const float Eb1 = (Sb - Bb[cc + 1]) / (Sa - Ba[cc + 1]) * inv_db;
+    const float Cb = (Sb - pb[0]) * inv_db;
+    const float invD = 1.0f / (Sa - Pa[cc]);
+    const float t1 = (Sb - Pb[cc]) * invD;
+    const float A = (Sz - pzp[0]) * inv_dz;
+    float Bj[kTR + 1];
+#pragma unroll
+    for (int j = 0; j <= kTR; ++j) Bj[j] = (Sz - Bzr[min(r0 + j, nv)]) * inv_dz;
+
+    // Per-slice tile window: the union of every lane's exact footprint cells
+    // (the same expressions the sweep evaluates, so every cell the sweep
+    // touches lies inside the window), widened by one cell.
+    auto window = [&](int s) {
+        TileWindow w;
+        const float q = pa[s] + 0.5f * da - Sa;
+        const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
+        const float tau = q * invD;
+        const float za = fmaf(Bj[0], tau, A), zb = fmaf(Bj[kTR], tau, A);
+        const int klo = __reduce_min_sync(0xffffffffu, (int)floorf(fminf(xa, xb))) - 1;
+        const int khi = __reduce_max_sync(0xffffffffu, (int)floorf(fmaxf(xa, xb))) + 1;
+        const int llo = __reduce_min_sync(0xffffffffu, (int)floorf(fminf(za, zb))) - 1;
+        const int lhi = __reduce_max_sync(0xffffffffu, (int)floorf(fmaxf(za, zb))) + 1;
+        w.active = !(khi < 0 || klo >= nB || lhi < 0 || llo >= nZ);
+        w.kb = (klo >= 0 ? klo : klo - 3) / 4 * 4;           // floor to a multiple of 4
+        w.lb = llo;
+        w.nbz = (lhi - llo + kBoxZ) / kBoxZ;
+        w.fits = TMA && (khi + 4 - w.kb <= kPX) && (w.nbz * kBoxZ <= kPZ);
+        return w;
+    };
+
+    if (lane == 0) {
+        mbar_init(&sm.bar[0], 1);
+        mbar_init(&sm.bar[1], 1);
+        fence_mbar_init();
+    }
+    // Zero both buffers once so that taps past the loaded boxes read finite zeros.
+    {
+        float4 *z = reinterpret_cast<float4 *>(&sm.buf[0][0][0]);
+        for (int i = lane; i < 2 * kPZ * kPX / 4; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncwarp();
+
+    float acc[kTR];
+#pragma unroll
+    for (int j = 0; j < kTR; ++j) acc[j] = 0.0f;
+    uint32_t phase_bits = 0u, pending_bits = 0u;   // bit b: phase parity / TMA outstanding for buffer b
+    bool failed = false;
+
+    auto issue = [&](int s, const TileWindow &w, int b) {
+        if (!(w.active && w.fits)) return;
+        if (lane == 0) {
+            mbar_arrive_expect_tx(&sm.bar[b], (uint32_t)(w.nbz * kBoxZ * kBoxX * 4));
+            for (int iz = 0; iz < w.nbz; ++iz)
+                tma_load_3d(&sm.buf[b][iz * kBoxZ][0], &tm, w.kb, s, w.lb + iz * kBoxZ, &sm.bar[b]);
+        }
+        pending_bits |= 1u << b;
+    };
+
+    TileWindow wcur = window(0);
+    issue(0, wcur, 0);
+    for (int s = 0; s < nA; ++s) {
+        const int b = s & 1;
+        TileWindow wnext;
+        if (s + 1 < nA) {
+            wnext = window(s + 1);
+            issue(s + 1, wnext, b ^ 1);
+        }
+        if (wcur.active) {
+            if ((pending_bits >> b) & 1u) {
+                if (!mbar_wait(&sm.bar[b], (phase_bits >> b) & 1u, status)) { failed = true; break; }
+                phase_bits ^= 1u << b;
+                pending_bits &= ~(1u << b);
+            }
+            const float q = pa[s] + 0.5f * da - Sa;
+            const float g = 1.0f / (q * q);
+            const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
+            const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
+            const float tau = q * invD;
+            float fk;
+            const int k0 = floor_split(lo, &fk);
+            const bool wide = __any_sync(0xffffffffu, (hi - fk) > 4.0f);
+            if (wcur.fits && !wide) {
+                float ov[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    ov[t] = fmaxf(0.0f, fminf(fk + (float)(t + 1), hi) - fmaxf(fk + (float)t, lo));
+                int ntl = 1;
+#pragma unroll
+                for (int t = 1; t < 4; ++t) ntl = (ov[t] > 0.0f) ? t + 1 : ntl;
+                PatchCells H;
+                H.base = &sm.buf[b][0][k0 - wcur.kb];
+                H.lb = wcur.lb;
+                H.nt = __reduce_max_sync(0xffffffffu, ntl);
+                H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
+                sweep_rows<kTR / 2>(H, Bj, A, tau, g, acc);
+                sweep_rows<kTR / 2>(H, Bj + kTR / 2, A, tau, g, acc + kTR / 2);
+            } else {
+                // Cell-by-cell overlap from global memory; row values go through
+                // shared memory so the row loop stays rolled (small code).
+                const float *__restrict__ slab = src + (long long)s * st_s;
+                const int ka = max(k0, 0), kz = min((int)floorf(hi), nB - 1);
+                for (int j = 0; j < kTR; ++j) {
+                    const float bja = (Sz - Bzr[min(r0 + j, nv)]) * inv_dz;
+                    const float bjb = (Sz - Bzr[min(r0 + j + 1, nv)]) * inv_dz;
+                    const float za = fmaf(bja, tau, A), zb = fmaf(bjb, tau, A);
+                    const float zlo = fminf(za, zb), zhi = fmaxf(za, zb);
+                    const int l0 = max((int)floorf(zlo), 0), l1 = min((int)floorf(zhi), nZ - 1);
+                    float v = 0.0f;
+                    for (int l = l0; l <= l1; ++l) {
+                        const float wz = fminf((float)(l + 1), zhi) - fmaxf((float)l, zlo);
+                        const float *__restrict__ row = slab + (long long)l * st_l;
+                        float hx = 0.0f;
+                        for (int k = ka; k <= kz; ++k)
+                            hx += __ldg(row + k * st_k) * (fminf((float)(k + 1), hi) - fmaxf((float)k, lo));
+                        v += hx * wz;
+                    }
+                    sm.spill[j][lane] = v;
+                }
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < kTR; ++j) acc[j] = fmaf(sm.spill[j][lane], g, acc[j]);
+            }
+        }
+        __syncwarp();
+        wcur = wnext;
+    }
+    if (failed) {
+        // Let copies still in flight land before the CTA exits (bounded).
+        for (int b = 0; b < 2; ++b)
+            if ((pending_bits >> b) & 1u) mbar_wait(&sm.bar[b], (phase_bits >> b) & 1u, status);
+        return;
+    }
+    if (c >= nu) return;
+    const float dEb = fabsf(Eb1 - Eb0);
+    const float absInvD = fabsf(invD);
+    const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (dEb * absInvD);
+#pragma unroll
+    for (int j = 0; j < kTR; ++j) {
+        const int r = r0 + j;
+        if (r < nv) {
+            const float t2 = (Sz - Pzr[r]) * invD;
+            const float K = base * sqrtf(1.0f + t2 * t2) / fabsf(Bj[j + 1] - Bj[j]);
+            proj[((long long)vi * nv + r) * nu + c] = acc[j] * K;
+        }
+    }
+}
+
 }  // namespace ctgb
 
 using namespace ctgb;
@@ -120,6 +384,25 @@ static int check_launch(const char *what) {
     return CTGB_OK;
 }
 
+// Dominant axis of each view, by the table builder's float64 rule
+// (distance_forward, python/Reconstruction_numba.py:896, :966).
+static void view_axes(const ctgb_params *p, int view0, int nviews, std::vector<int> &axes) {
+    const double *S0 = p->source_init, *D0 = p->detector_init, *O = p->rotation_origin;
+    const double sad = std::sqrt((S0[0] - O[0]) * (S0[0] - O[0]) + (S0[1] - O[1]) * (S0[1] - O[1]) +
+                                 (S0[2] - O[2]) * (S0[2] - O[2]));
+    const double sdd = std::sqrt((S0[0] - D0[0]) * (S0[0] - D0[0]) + (S0[1] - D0[1]) * (S0[1] - D0[1]) +
+                                 (S0[2] - D0[2]) * (S0[2] - D0[2]));
+    const double step = (p->end_angle - p->start_angle) / p->nviews;
+    axes.resize(nviews);
+    for (int i = 0; i < nviews; ++i) {
+        const double th = (view0 + i) * step + p->start_angle;
+        const double S[3] = {-sad * std::sin(th), sad * std::cos(th), p->source_init[2]};
+        const double D[3] = {(sdd - sad) * std::sin(th), -(sdd - sad) * std::cos(th), p->detector_init[2]};
+        const double ax = std::fabs(S[0] - D[0]), ay = std::fabs(S[1] - D[1]), az = std::fabs(S[2] - D[2]);
+        axes[i] = (ax >= ay && ax >= az) ? 0 : (ay >= ax && ay >= az) ? 1 : 2;
+    }
+}
+
 extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                             float *d_proj, int32_t view0, int32_t nviews, void *stream) {
     clear_error();
@@ -128,15 +411,85 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
         return set_error(CTGB_ERR_ARG, "ctgb_forward: view range [%d,%d) outside [0,%d)", view0, view0 + nviews,
                          p->nviews);
     if (nviews == 0) return CTGB_OK;
-    dim3 block(kFwdTileU, kFwdTileV);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    for (int v = 0; v < nviews; v += 65535) {
-        int nv_chunk = nviews - v < 65535 ? nviews - v : 65535;
-        dim3 grid((p->nu + kFwdTileU - 1) / kFwdTileU, (p->nv + kFwdTileV - 1) / kFwdTileV, nv_chunk);
-        dd_forward_kernel<<<grid, block, 0, st>>>(static_cast<const float *>(d_table), d_vol, d_vol_xzy,
-                                                  d_proj + (long long)v * p->nu * p->nv, view0 + v);
+    const float *T = static_cast<const float *>(d_table);
+    const long long view_elems = (long long)p->nu * p->nv;
+
+    // x/y-dominant views run dd_forward_tma_kernel (TMA patches when the
+    // volume layout allows 16-byte row strides, global loads otherwise);
+    // z-dominant views run the per-pixel kernel.
+    CUtensorMap tm_y, tm_x;
+    const uint32_t box[3] = {kBoxX, 1, kBoxZ};
+    bool tma_y = (p->nx % 4 == 0), tma_x = (p->ny % 4 == 0) && d_vol_xzy != nullptr;
+    if (tma_y) {
+        const uint64_t d[3] = {(uint64_t)p->nx, (uint64_t)p->ny, (uint64_t)p->nz};
+        tma_y = ctgb_make_tmap_3d(&tm_y, d_vol, d, box);
     }
-    return check_launch("dd_forward_kernel");
+    if (tma_x) {
+        const uint64_t d[3] = {(uint64_t)p->ny, (uint64_t)p->nx, (uint64_t)p->nz};
+        tma_x = ctgb_make_tmap_3d(&tm_x, d_vol_xzy, d, box);
+    }
+    if (!tma_y) std::memset(&tm_y, 0, sizeof tm_y);
+    if (!tma_x) std::memset(&tm_x, 0, sizeof tm_x);
+    int *status = ctgb_status_ptr();
+    if (!status) return set_error(CTGB_ERR_CUDA, "ctgb_forward: device status word unavailable");
+    const int smem = (int)sizeof(FwdTmaSmem);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaSuccess;
+        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<true, true>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
+        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<false, true>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
+        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<true, false>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
+        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<false, false>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "dd_forward smem attribute: %s", cudaGetErrorString(e));
+        attr_set = true;
+    }
+    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + kTR - 1) / kTR;
+    const bool tiles_ok = (long long)ntu * ntv <= 65535;
+    const float *src_x = d_vol_xzy ? d_vol_xzy : d_vol;
+    const long long stk_x = d_vol_xzy ? 1LL : (long long)p->nx;
+
+    // Runs of consecutive views that take the same kernel.
+    std::vector<int> axes;
+    view_axes(p, view0, nviews, axes);
+    int i = 0;
+    while (i < nviews) {
+        const int a = (axes[i] == 2 || !tiles_ok) ? 2 : axes[i];
+        int j = i + 1;
+        while (j < nviews && ((axes[j] == 2 || !tiles_ok) ? 2 : axes[j]) == a) ++j;
+        for (int v = i; v < j; v += 65535) {
+            const int n = (j - v) < 65535 ? (j - v) : 65535;
+            if (a == 2) {
+                dim3 block(kFwdTileU, kFwdTileV);
+                dim3 grid((p->nu + kFwdTileU - 1) / kFwdTileU, (p->nv + kFwdTileV - 1) / kFwdTileV, n);
+                dd_forward_kernel<<<grid, block, 0, st>>>(T, d_vol, d_vol_xzy, d_proj + (long long)v * view_elems,
+                                                          view0 + v);
+            } else {
+                dim3 grid(n, ntu * ntv);
+                if (a == 0) {
+                    if (tma_x)
+                        dd_forward_tma_kernel<true, true><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj,
+                                                                                  view0, v, ntu, status);
+                    else
+                        dd_forward_tma_kernel<true, false><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj,
+                                                                                   view0, v, ntu, status);
+                } else {
+                    if (tma_y)
+                        dd_forward_tma_kernel<false, true><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj,
+                                                                                   view0, v, ntu, status);
+                    else
+                        dd_forward_tma_kernel<false, false><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj,
+                                                                                    view0, v, ntu, status);
+                }
+            }
+        }
+        i = j;
+    }
+    return check_launch("dd_forward");
 }
 
 extern "C" int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t ny, int32_t nz,

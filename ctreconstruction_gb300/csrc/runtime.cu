@@ -1,0 +1,69 @@
+// Runtime helpers: the device status word, TMA descriptor construction.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include "status.h"
+#include "tma.cuh"
+
+namespace ctgb {
+__device__ int g_device_status = 0;
+}
+
+int *ctgb_status_ptr() {
+    static int *ptrs[64] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, ctgb::g_device_status) != cudaSuccess) return nullptr;
+        ptrs[dev] = static_cast<int *>(p);
+    }
+    return ptrs[dev];
+}
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+bool ctgb_make_tmap_3d(CUtensorMap *map, const float *base, const uint64_t dims[3], const uint32_t box[3]) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t gdim[3] = {dims[0], dims[1], dims[2]};
+    cuuint64_t gstride[2] = {dims[0] * 4, dims[0] * dims[1] * 4};
+    cuuint32_t bdim[3] = {box[0], box[1], box[2]};
+    cuuint32_t estride[3] = {1, 1, 1};
+    if ((gstride[0] % 16) || (gstride[1] % 16) || (reinterpret_cast<uintptr_t>(base) % 16)) return false;
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), gdim, gstride, bdim, estride,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// Reads (and optionally clears) the device status word of the current device.
+// Synchronises the device.  *out = 0 when no kernel reported a problem.
+extern "C" int ctgb_device_status(int32_t *out, int32_t clear) {
+    ctgb::clear_error();
+    if (!out) return ctgb::set_error(CTGB_ERR_ARG, "ctgb_device_status: out is NULL");
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, ctgb::g_device_status, sizeof(int));
+    if (e != cudaSuccess) return ctgb::set_error(CTGB_ERR_CUDA, "ctgb_device_status: %s", cudaGetErrorString(e));
+    if (clear && v) {
+        int z = 0;
+        e = cudaMemcpyToSymbol(ctgb::g_device_status, &z, sizeof(int));
+        if (e != cudaSuccess) return ctgb::set_error(CTGB_ERR_CUDA, "ctgb_device_status: %s", cudaGetErrorString(e));
+    }
+    *out = v;
+    return CTGB_OK;
+}

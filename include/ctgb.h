@@ -101,7 +101,14 @@ int ctgb_filter_bytes(const ctgb_params *p, size_t *bytes);
 int ctgb_filter_build(const ctgb_params *p, int32_t filter_type, double cutoff, void *host_buf, size_t bytes);
 int ctgb_fdk_filter(const ctgb_params *p, const void *d_filter, float *d_proj, int32_t nviews, void *stream);
 
-/* ---- status ---------------------------------------------------------------- */
+/* ---- status ----------------------------------------------------------------
+ * ctgb_device_status: the device-side status word of the current device
+ * (CTGB_DEVERR_* bits set by kernels whose bounded waits ran out).  Reads it
+ * with a synchronous copy (so it synchronises the device) and optionally
+ * clears it.  No reference counterpart (the reference has no device-side
+ * error reporting). */
+#define CTGB_DEVERR_TIMEOUT 1
+int ctgb_device_status(int32_t *out, int32_t clear);
 const char *ctgb_last_error(void);
 const char *ctgb_version(void);
 

@@ -68,6 +68,18 @@ GEOMS = {
     "curved": cone_params(n=18, nviews=12, nu=36, nv=24, DetectorShape='Curved'),
     "pycuda_offset": dict(cone_params(n=(19, 15, 11), nviews=11, nu=33, nv=21, ReconCenter=[0.3, -0.2, 0.5]),
                           DetectorOffset=[0.6, -0.45]),
+    # sizes with nx, ny multiples of 4 take the TMA forward path
+    "tma_cone": cone_params(n=(32, 28, 20), nviews=20, nu=48, nv=40, dx=0.8),
+    "tma_offcentre": cone_params(n=(36, 24, 22), nviews=17, nu=56, nv=36, start=0.3, span=2 * np.pi,
+                                 PhantomCenter=[2.1, -1.3, 0.9], ReconCenter=[-0.6, 0.8, -0.3]),
+    "tma_fine": cone_params(n=(24, 24, 16), nviews=12, nu=100, nv=70, du=0.3, dv=0.35),
+    "tma_wide_footprint": cone_params(n=(28, 32, 24), nviews=12, nu=12, nv=10, du=5.0, dv=4.5),
+    "tma_tall_rows": cone_params(n=(24, 24, 48), nviews=10, nu=40, nv=20, du=1.0, dv=3.2),
+    "tma_curved": cone_params(n=(28, 24, 20), nviews=14, nu=44, nv=32, DetectorShape='Curved'),
+    "tma_helical": cone_params(n=(24, 24, 20), nviews=18, nu=40, nv=20, Pitch=0.6, span=4 * np.pi),
+    "tma_pycuda": dict(cone_params(n=(32, 20, 14), nviews=9, nu=36, nv=24, ReconCenter=[0.5, 0.2, -0.4]),
+                       DetectorOffset=[-0.7, 0.35]),
+    "tma_partial_tiles": cone_params(n=(20, 28, 18), nviews=11, nu=45, nv=27),
 }
 
 
@@ -85,7 +97,7 @@ def test_against_fp64_oracle(cuda, gname):
     assert rel_err(P.backproject_matched(_t(y, cuda)).cpu().numpy(), g.backward_matched(y)) < RTOL
 
 
-@pytest.mark.parametrize("gname", ["cone_y_and_x_views", "curved", "helical"])
+@pytest.mark.parametrize("gname", ["cone_y_and_x_views", "curved", "helical", "tma_cone", "tma_curved"])
 def test_matched_backprojector_is_adjoint(cuda, gname):
     """Dot-product test <A x, y> = <x, A^T y> to 1e-5 relative."""
     p = GEOMS[gname]
@@ -98,8 +110,9 @@ def test_matched_backprojector_is_adjoint(cuda, gname):
     assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
 
 
-def test_forward_without_transposed_copy_matches(cuda):
-    p = GEOMS["cone_y_and_x_views"]
+@pytest.mark.parametrize("gname", ["cone_y_and_x_views", "tma_cone"])
+def test_forward_without_transposed_copy_matches(cuda, gname):
+    p = GEOMS[gname]
     P = Projector(p)
     x = torch.rand(P.volume_shape, device=cuda)
     a = P.forward(x)
@@ -110,7 +123,7 @@ def test_forward_without_transposed_copy_matches(cuda):
               None, ctypes.c_void_p(b.data_ptr()), 0, P.params.NumberOfViews,
               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
-    assert torch.equal(a, b)
+    assert rel_err(b.cpu().numpy(), a.cpu().numpy()) < 1e-5
 
 
 def test_view_ranges_and_accumulate(cuda):
@@ -127,8 +140,9 @@ def test_view_ranges_and_accumulate(cuda):
     assert rel_err(acc.cpu().numpy(), whole.cpu().numpy()) < 1e-6
 
 
-def test_deterministic(cuda):
-    p = GEOMS["offcentre_short_scan"]
+@pytest.mark.parametrize("gname", ["offcentre_short_scan", "tma_offcentre"])
+def test_deterministic(cuda, gname):
+    p = GEOMS[gname]
     P = Projector(p)
     x = torch.rand(P.volume_shape, device=cuda)
     y = torch.rand(P.proj_shape(), device=cuda)
@@ -145,3 +159,12 @@ def test_bad_inputs_raise(cuda):
         P.forward(torch.rand(P.volume_shape, device=cuda, dtype=torch.float64))
     with pytest.raises(ValueError):
         P.forward(torch.rand((3, 3, 3), device=cuda))
+
+
+def test_device_status_clean_after_runs(cuda):
+    """No kernel reported a wait timeout or bounds problem."""
+    import ctypes
+    from ctreconstruction_gb300 import _lib
+    st = ctypes.c_int32(-1)
+    _lib.call("ctgb_device_status", ctypes.byref(st), 1)
+    assert st.value == 0
