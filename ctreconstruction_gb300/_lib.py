@@ -34,6 +34,7 @@ SIGNATURES = {
     "ctgb_table_bytes": [_P, ctypes.POINTER(_sz)],
     "ctgb_table_build": [_P, _vp, _sz],
     "ctgb_forward": [_P, _vp, _vp, _vp, _vp, _i32, _i32, _vp],
+    "ctgb_forward_static": [_P, _vp, _vp, _vp, _i32, _i32, _vp],
     "ctgb_transpose_xy": [_vp, _vp, _i32, _i32, _i32, _vp],
     "ctgb_backproject_fdk": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_backproject_matched": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],

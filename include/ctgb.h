@@ -71,6 +71,20 @@ int ctgb_table_build(const ctgb_params *p, void *host_table, size_t bytes);
 int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                  float *d_proj, int32_t view0, int32_t nviews, void *stream);
 
+/* Same result as ctgb_forward, for callers that cannot allocate device
+ * memory where they project (an application whose own pool owns the device
+ * memory budget, or a latency-bound loop that cannot take cudaMalloc's
+ * device-wide synchronisation).  No counterpart in the reference.  Instead of
+ * a caller-allocated d_vol_xzy it uses a file-scope __device__ array of
+ * CTGB_STATIC_MAX_VOXELS floats (16 MiB, held by every GPU that loads the
+ * library until exit); larger volumes are rejected with CTGB_ERR_SIZE.  The
+ * first call on a device looks up that array's address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race on it. */
+#define CTGB_STATIC_MAX_VOXELS (1 << 22)
+int ctgb_forward_static(const ctgb_params *p, const void *d_table, const float *d_vol, float *d_proj,
+                        int32_t view0, int32_t nviews, void *stream);
+
 /* vol_xzy[z][x][y] = vol[z][y][x]. */
 int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t ny, int32_t nz, void *stream);
 
