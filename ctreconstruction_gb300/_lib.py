@@ -27,6 +27,24 @@ class CtgbParams(ctypes.Structure):
                 ("pitch", ctypes.c_double), ("curved", ctypes.c_int32), ("flavour", ctypes.c_int32)]
 
 
+class CtgbConeBeamParams(ctypes.Structure):
+    """Mirror of ``ctgb_conebeam_params`` (include/ctgb.h)."""
+    _fields_ = [("source_to_axis", ctypes.c_double), ("source_to_detector", ctypes.c_double),
+                ("pixel_width", ctypes.c_double), ("pixel_height", ctypes.c_double),
+                ("det_width", ctypes.c_int32), ("det_height", ctypes.c_int32), ("nviews", ctypes.c_int32),
+                ("angle_coverage", ctypes.c_double), ("recon_x", ctypes.c_int32), ("recon_y", ctypes.c_int32),
+                ("recon_z", ctypes.c_int32), ("arc", ctypes.c_int32)]
+
+
+class CtgbFanSlice(ctypes.Structure):
+    """Mirror of ``ctgb_fan_slice`` (include/ctgb.h)."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("x0", ctypes.c_float), ("dx", ctypes.c_float),
+                ("y0", ctypes.c_float), ("dy", ctypes.c_float), ("R", ctypes.c_float), ("D", ctypes.c_float),
+                ("g0", ctypes.c_float), ("dg", ctypes.c_float), ("nch", ctypes.c_int32), ("nviews", ctypes.c_int32),
+                ("theta0", ctypes.c_float), ("dtheta", ctypes.c_float), ("arc", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("sino_offset", ctypes.c_int64), ("image_offset", ctypes.c_int64)]
+
+
 # (name, argtypes); every entry point returns int status except the string getters.
 _P = ctypes.POINTER(CtgbParams)
 _vp, _i32, _f32, _sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float, ctypes.c_size_t
@@ -38,10 +56,31 @@ SIGNATURES = {
     "ctgb_transpose_xy": [_vp, _vp, _i32, _i32, _i32, _vp],
     "ctgb_backproject_fdk": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_backproject_matched": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
+    "ctgb_backproject_fdk_workspace_bytes": [_P, _i32, ctypes.POINTER(_sz)],
+    "ctgb_backproject_fdk_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],
     "ctgb_filter_bytes": [_P, ctypes.POINTER(_sz)],
     "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],
     "ctgb_fdk_filter": [_P, _vp, _vp, _i32, _vp],
     "ctgb_device_status": [ctypes.POINTER(_i32), _i32],
+    "ctgb_partials_count": [ctypes.c_int64, ctypes.POINTER(_i32)],
+    "ctgb_sart_residual": [_vp, _vp, _vp, _f32, _vp, ctypes.c_int64, _vp],
+    "ctgb_sart_update": [_vp, _vp, _vp, _f32, _f32, _vp, ctypes.c_int64, _vp],
+    "ctgb_em_ratio": [_vp, _vp, _f32, _vp, ctypes.c_int64, _vp],
+    "ctgb_em_update": [_vp, _vp, _vp, _vp, ctypes.c_int64, _vp],
+    "ctgb_pocs_residual": [_vp, _vp, _vp, _f32, _vp, ctypes.c_int64, _vp],
+    "ctgb_pocs_update": [_vp, _vp, _vp, _f32, _f32, _vp, ctypes.c_int64, _vp],
+    "ctgb_tv_step": [_vp, _vp, _i32, _i32, _i32, _f32, _f32, _vp, _vp],
+    "ctgb_sqdist": [_vp, _vp, ctypes.c_int64, _vp, _vp, _vp],
+    "ctgb_conebeam_table_bytes": [ctypes.POINTER(CtgbConeBeamParams), ctypes.POINTER(_sz)],
+    "ctgb_conebeam_table_build": [ctypes.POINTER(CtgbConeBeamParams), _vp, _sz],
+    "ctgb_conebeam_backproject": [ctypes.POINTER(CtgbConeBeamParams), _vp, _vp, _vp, _i32, _i32, _i32, _vp],
+    "ctgb_standalone_filter_bytes": [ctypes.POINTER(CtgbConeBeamParams), ctypes.POINTER(_sz)],
+    "ctgb_standalone_filter_build": [ctypes.POINTER(CtgbConeBeamParams), _i32, _i32, ctypes.c_double, _vp, _sz],
+    "ctgb_filter_apply": [_vp, _i32, _vp, ctypes.c_int64, _vp],
+    "ctgb_filter_zpl": [_vp, ctypes.POINTER(_i32)],
+    "ctgb_fan_batch_bytes": [ctypes.POINTER(CtgbFanSlice), _i32, _i32, _i32, ctypes.POINTER(_sz)],
+    "ctgb_fan_batch_build": [ctypes.POINTER(CtgbFanSlice), _i32, _i32, _i32, _vp, _sz],
+    "ctgb_fan_backproject": [_vp, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _vp],
 }
 STRING_FUNCS = ("ctgb_last_error", "ctgb_version")
 

@@ -216,6 +216,218 @@ bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj,
     }
 }
 
+// ---------------------------------------------------------------------------
+// FDK-weighted DD backprojection over integrated projections (default when
+// the caller supplies a workspace).
+//
+// integrate_rows_kernel writes, per view and detector column l, the running
+// sums C(m) = sum_{m' < m} Q[m'][l] (m = 0..nv) next to Q itself as float2
+// (C, Q) — the "integrated" projections.  The integral of the piecewise
+// constant column over any row interval [a, b] is then
+// (C + Q frac)(b) - (C + Q frac)(a): two lookups, whatever the footprint's
+// size.  The backprojector (one thread per voxel column x 16 voxels, all views
+// in registers) does, per voxel and view, two lookups per u cell of the
+// column's footprint; within a 16-voxel chunk that does not straddle the
+// source height the v footprint ends move linearly with z, so they are one
+// FMA each.  Running sums are accumulated in double and stored rounded, so
+// each lookup carries one float32 rounding of the prefix, not a drifting sum.
+constexpr int kBiZ = 16;
+
+__global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__restrict__ out, int nu, int nv,
+                                      int nviews) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * nviews) return;
+    const int v = (int)(t / nu), l = (int)(t % nu);
+    const float *__restrict__ q = proj + (long long)v * nu * nv + l;
+    float2 *__restrict__ o = out + (long long)v * (nv + 1) * nu + l;
+    double c = 0.0;
+    for (int m = 0; m < nv; ++m) {
+        const float x = __ldg(q + (long long)m * nu);
+        o[(long long)m * nu] = make_float2((float)c, x);
+        c += x;
+    }
+    o[(long long)nv * nu] = make_float2((float)c, 0.0f);
+}
+
+template <int NT>
+__device__ __forceinline__ float integ_taps(const float2 *__restrict__ rlo, const float2 *__restrict__ rhi,
+                                            float flo, float fhi, const float *ov) {
+    float s = 0.0f;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const float2 a = __ldg(rlo + t), b = __ldg(rhi + t);
+        s = fmaf(ov[t], fmaf(b.y, fhi, b.x) - fmaf(a.y, flo, a.x), s);
+    }
+    return s;
+}
+
+template <int NT, bool LINEAR>
+__device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int nu, int nv, int lbase,
+                                             const float *ov, float zfirst, float dzs, float hz, float Sz, float imin,
+                                             float imax, float Mv, float Av, float wscale, float *acc) {
+    const float fnv = (float)nv;
+    float lo0, hi0, dlo = 0.0f, dhi = 0.0f;
+    v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &lo0, &hi0);
+    if (LINEAR) {
+        float lo1, hi1;
+        v_footprint(zfirst + dzs, hz, Sz, imin, imax, Mv, Av, &lo1, &hi1);
+        dlo = lo1 - lo0;
+        dhi = hi1 - hi0;
+    }
+#pragma unroll
+    for (int j = 0; j < kBiZ; ++j) {
+        float vlo, vhi;
+        if (LINEAR) {
+            vlo = fmaf((float)j, dlo, lo0);
+            vhi = fmaf((float)j, dhi, hi0);
+        } else {
+            v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &vlo, &vhi);
+        }
+        const float width = vhi - vlo;
+        const float clo = fminf(fmaxf(vlo, 0.0f), fnv), chi = fminf(fmaxf(vhi, 0.0f), fnv);
+        float flo, fhi;
+        const int mlo = floor_split(clo, &flo), mhi = floor_split(chi, &fhi);
+        const float2 *rlo = IQ + (long long)mlo * nu + lbase;
+        const float2 *rhi = IQ + (long long)mhi * nu + lbase;
+        const float integ = integ_taps<NT>(rlo, rhi, clo - flo, chi - fhi, ov);
+        // A footprint narrower than a detector row lies in one row: weight 1.
+        const float val = (width > 1e-6f) ? integ * fast_rcp(width) : integ_taps<NT>(rlo, rlo, 0.0f, 1.0f, ov);
+        acc[j] = fmaf(val, wscale, acc[j]);
+    }
+}
+
+template <bool CURVED>
+__global__ void __launch_bounds__(kBpTX * kBpTY, 6)
+bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ, float *__restrict__ vol,
+                    int view0, int nviews, float scale, int accumulate) {
+    const TableHeader &h = header(T);
+    const int ix = blockIdx.x * kBpTX + threadIdx.x;
+    const int iy = blockIdx.y * kBpTY + threadIdx.y;
+    const int z0 = blockIdx.z * kBiZ;
+    const bool live = ix < h.nx && iy < h.ny;
+    const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
+    const float *__restrict__ ki = T + h.off_ki;
+    const float *__restrict__ pp = T + h.off_pp;
+    const int nu = h.nu, nv = h.nv, nz = h.nz;
+    const float xx = T[h.off_xpix + ixc], yy = T[h.off_ypix + iyc];
+    const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f, dzs = h.dz;
+    const float du = h.du_bp, dv = h.dv_bp, inv_du = 1.0f / du, inv_dv = 1.0f / dv;
+    const float ki0 = ki[0], pp0 = pp[0];
+    const float Sx = h.src0x, Sy = h.src0y, Dy = h.det0y, R = h.sad;
+    const float eps = h.eps_bp;
+    const float zfirst = T[h.off_zpix + min(z0, nz - 1)];
+    const int zlast = min(z0 + kBiZ, nz) - 1 - z0;
+    const float zend = zfirst + (float)zlast * dzs;
+    float acc[kBiZ];
+#pragma unroll
+    for (int j = 0; j < kBiZ; ++j) acc[j] = 0.0f;
+
+    for (int vi = 0; vi < nviews; ++vi) {
+        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+        const float cs = V[VF_COS], sn = V[VF_SIN], Sz = V[VF_BPSZ];
+        const float2 *__restrict__ IQ = integ + (long long)vi * (nv + 1) * nu;
+        const float yc = yy * cs - xx * sn;
+        float umin = INFINITY, umax = -INFINITY, imin = INFINITY, imax = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float cx = xx + ((q & 1) ? hx : -hx), cy = yy + ((q & 2) ? hy : -hy);
+            const float xr = cx * cs + cy * sn, yr = cy * cs - cx * sn;
+            const float inv = fast_rcp(Sy - yr);
+            const float su = (Sx - xr) * inv;
+            umin = fminf(umin, su); umax = fmaxf(umax, su);
+            imin = fminf(imin, inv); imax = fmaxf(imax, inv);
+        }
+        float cu1, cu2;
+        if (CURVED) { cu1 = -atanf(umin); cu2 = -atanf(umax); }
+        else { cu1 = fmaf(umin, Dy - Sy, Sx); cu2 = fmaf(umax, Dy - Sy, Sx); }
+        const float ua = (cu1 - ki0) * inv_du, ub = (cu2 - ki0) * inv_du;
+        const float ulo = fminf(ua, ub), uhi = fmaxf(ua, ub);
+        float fl0;
+        const int l0 = floor_split(ulo, &fl0);
+        const float uw = uhi - ulo;
+        const float Rd = R - yc;
+        float wscale = scale * (R * R) * fast_rcp(Rd * Rd);
+        float ov[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int l = l0 + t;
+            const float o = fmaxf(0.0f, fminf(fl0 + (float)(t + 1), uhi) - fmaxf(fl0 + (float)t, ulo));
+            ov[t] = (l >= 0 && l < nu) ? o : 0.0f;   // cells off the detector add nothing
+        }
+        if (uw > 1e-6f) wscale *= fast_rcp(uw);
+        else { ov[0] = (l0 >= 0 && l0 < nu) ? 1.0f : 0.0f; ov[1] = ov[2] = ov[3] = 0.0f; }
+        // Clamp the tap base so every tap address lies inside the detector row.
+        const int lbase = min(max(l0, 0), max(nu - 4, 0));
+        // Weights re-aligned to the clamped base: tap t reads cell lbase + t,
+        // whose weight is ov[lbase + t - l0] (a select chain, not an indexed load).
+        const int shift = lbase - l0;
+        float ovb[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int src = t + shift;
+            float w = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) w = (src == k) ? ov[k] : w;
+            ovb[t] = w;
+        }
+        int ntl = 1;
+#pragma unroll
+        for (int t = 1; t < 4; ++t) ntl = (ovb[t] > 0.0f) ? t + 1 : ntl;
+        const bool ok = live && imin > 0.0f && (uhi - fl0) <= 4.0f && nu >= 4;
+        const int nt = __reduce_max_sync(0xffffffffu, ok ? ntl : 1);
+        const float Mv = (Dy - Sy) * inv_dv, Av = (Sz - pp0) * inv_dv;
+        // Linear z regime: neither z end of any voxel in the chunk crosses S_z.
+        const float ztop = fmaxf(zfirst, zend) + fabsf(hz), zbot = fminf(zfirst, zend) - fabsf(hz);
+        const bool linear = (Sz - ztop > 0.0f) || (Sz - zbot < 0.0f);
+        if (ok) {
+            if (linear) {
+                if (nt <= 2) integ_voxels<2, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+                else if (nt == 3) integ_voxels<3, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+                else integ_voxels<4, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+            } else {
+                integ_voxels<4, false>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+            }
+        } else if (live) {
+            // Reference weight calculators on the raw values (Q = the float2's y).
+            const Span us = make_span(cu1, cu2, ki0, inv_du);
+            const int c0 = max(us.s, 0), c1 = min(us.e, nu - 1);
+            const float abs_du = fabsf(du), abs_dv = fabsf(dv);
+            const float Wd = scale * (R * R) / (Rd * Rd);
+#pragma unroll
+            for (int j = 0; j < kBiZ; ++j) {
+                if (j > zlast) break;
+                const float zc = zfirst + (float)j * dzs;
+                const float nlo = Sz - (zc - hz), nhi = Sz - (zc + hz);
+                const float a0 = nlo * imin, a1 = nlo * imax, a2 = nhi * imin, a3 = nhi * imax;
+                const float vmn = fminf(fminf(a0, a1), fminf(a2, a3));
+                const float vmx = fmaxf(fmaxf(a0, a1), fmaxf(a2, a3));
+                const float cv1 = fmaf(vmn, Dy - Sy, Sz), cv2 = fmaf(vmx, Dy - Sy, Sz);
+                const Span vs = make_span(cv1, cv2, pp0, inv_dv);
+                const int k0 = max(vs.s, 0), k1 = min(vs.e, nv - 1);
+                float sum = 0.0f;
+                for (int k = k0; k <= k1; ++k) {
+                    const float w1 = span_weight<true>(vs, k, pp[k], pp[k + 1], abs_dv, eps);
+                    const float2 *__restrict__ qrow = IQ + (long long)k * nu;
+                    float part = 0.0f;
+                    for (int l = c0; l <= c1; ++l)
+                        part += __ldg(qrow + l).y * span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
+                    sum += part * w1;
+                }
+                acc[j] = fmaf(sum, Wd, acc[j]);
+            }
+        }
+    }
+    if (!live) return;
+#pragma unroll
+    for (int j = 0; j < kBiZ; ++j) {
+        const int iz = z0 + j;
+        if (iz < nz) {
+            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
+            *dst = accumulate ? *dst + acc[j] : acc[j];
+        }
+    }
+}
+
 // ---- matched (adjoint) backprojector ---------------------------------------
 
 template <int A>
@@ -481,5 +693,51 @@ extern "C" int ctgb_backproject_matched(const ctgb_params *p, const void *d_tabl
         static_cast<const float *>(d_table), d_proj, d_vol, view0, nviews, scale, accumulate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_backproject_fdk_workspace_bytes(const ctgb_params *p, int32_t nviews, size_t *bytes) {
+    clear_error();
+    if (!p || !bytes || nviews < 0 || p->nu < 1 || p->nv < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_workspace_bytes: bad arguments");
+    *bytes = (size_t)nviews * (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                                       int32_t view0, int32_t nviews, float scale, int32_t accumulate,
+                                       void *d_workspace, size_t workspace_bytes, void *stream) {
+    clear_error();
+    int st = bp_args(p, d_table, d_proj, d_vol, view0, nviews, "ctgb_backproject_fdk_ws");
+    if (st) return st;
+    if (!d_workspace) return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_ws: NULL workspace");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nviews == 0) {
+        if (!accumulate) {
+            cudaError_t e = cudaMemsetAsync(d_vol, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nz, s);
+            if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
+        return CTGB_OK;
+    }
+    const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    const int chunk = (int)(workspace_bytes / per_view);
+    if (chunk < 1) return set_error(CTGB_ERR_SIZE, "ctgb_backproject_fdk_ws: workspace below one view");
+    const float *T = static_cast<const float *>(d_table);
+    float2 *ws = static_cast<float2 *>(d_workspace);
+    dim3 block(kBpTX, kBpTY);
+    dim3 grid((p->nx + kBpTX - 1) / kBpTX, (p->ny + kBpTY - 1) / kBpTY, (p->nz + kBiZ - 1) / kBiZ);
+    for (int v = 0; v < nviews; v += chunk) {
+        const int n = nviews - v < chunk ? nviews - v : chunk;
+        const long long threads = (long long)p->nu * n;
+        integrate_rows_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+            d_proj + (long long)v * p->nu * p->nv, ws, p->nu, p->nv, n);
+        const int acc = (v > 0) ? 1 : accumulate;
+        if (p->curved)
+            bp_fdk_integ_kernel<true><<<grid, block, 0, s>>>(T, ws, d_vol, view0 + v, n, scale, acc);
+        else
+            bp_fdk_integ_kernel<false><<<grid, block, 0, s>>>(T, ws, d_vol, view0 + v, n, scale, acc);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_integ_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
 }

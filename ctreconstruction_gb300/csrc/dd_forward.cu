@@ -151,23 +151,26 @@ struct TileWindow {
     bool active, fits;
 };
 
-// h(m): the lane's column footprint applied to patch row m.
+// h(m): the lane's column footprint (NT taps) applied to patch row m.
+template <int NT>
 struct PatchCells {
     const float *base;   // &patch[0][k0 - kb]
-    int lb, nt;
+    int lb;
     float ov0, ov1, ov2, ov3;
     __device__ __forceinline__ float operator()(int m) const {
         const float *p = base + (m - lb) * kPX;
         float v = p[0] * ov0 + p[1] * ov1;
-        if (nt > 2) v += p[2] * ov2;
-        if (nt > 3) v += p[3] * ov3;
+        if (NT > 2) v = fmaf(p[2], ov2, v);
+        if (NT > 3) v = fmaf(p[3], ov3, v);
         return v;
     }
 };
 
-// Integrate h over consecutive row boundaries of one chain of N rows.
-template <int N>
-__device__ __forceinline__ void sweep_rows(const PatchCells &H, const float *Bj, float A, float tau, float g,
+// Integrate h over consecutive row boundaries of one chain of N rows.  MID:
+// a row may cover three cells (one whole cell in the middle); rows never
+// cover four (checked per slice by the caller).  No data-dependent branches.
+template <int NT, bool MID, int N>
+__device__ __forceinline__ void sweep_rows(const PatchCells<NT> &H, const float *Bj, float A, float tau, float g,
                                            float *acc) {
     float f0;
     const float z0 = fmaf(Bj[0], tau, A);
@@ -182,12 +185,24 @@ __device__ __forceinline__ void sweep_rows(const PatchCells &H, const float *Bj,
         const float h1 = H(m1);
         const float e1 = h1 * (z1 - f1);
         float whole = (m1 > m0) ? h0 : 0.0f;
-        if (__any_sync(0xffffffffu, m1 > m0 + 1)) {
-            for (int m = m0 + 1; m < m1; ++m) whole += H(m);
+        if (MID) {
+            const float hm = H(m0 + 1);
+            whole += (m1 > m0 + 1) ? hm : 0.0f;
         }
         acc[j] = fmaf(whole + e1 - e0, g, acc[j]);
         m0 = m1; h0 = h1; e0 = e1;
     }
+}
+
+template <int NT, bool MID>
+__device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const float *Bj, float A,
+                                           float tau, float g, float *acc) {
+    PatchCells<NT> H;
+    H.base = patch;
+    H.lb = lb;
+    H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
+    sweep_rows<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
+    sweep_rows<NT, MID, kTR / 2>(H, Bj + kTR / 2, A, tau, g, acc + kTR / 2);
 }
 
 template <bool XD, bool TMA>
@@ -235,6 +250,9 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     float Bj[kTR + 1];
 #pragma unroll
     for (int j = 0; j <= kTR; ++j) Bj[j] = (Sz - Bzr[min(r0 + j, nv)]) * inv_dz;
+    float rowspan_max = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kTR; ++j) rowspan_max = fmaxf(rowspan_max, fabsf(Bj[j + 1] - Bj[j]));
 
     // Per-slice tile window: the union of every lane's exact footprint cells
     // (the same expressions the sweep evaluates, so every cell the sweep
@@ -307,22 +325,30 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
             const float tau = q * invD;
             float fk;
             const int k0 = floor_split(lo, &fk);
-            const bool wide = __any_sync(0xffffffffu, (hi - fk) > 4.0f);
+            // Row extent in cells: |B_{j+1} - B_j| * |tau|, at most rowspan_max * |tau|.
+            const float rows_ext = rowspan_max * fabsf(tau);
+            const bool wide = __any_sync(0xffffffffu, (hi - fk) > 4.0f || rows_ext > 1.99f);
             if (wcur.fits && !wide) {
                 float ov[4];
 #pragma unroll
                 for (int t = 0; t < 4; ++t)
                     ov[t] = fmaxf(0.0f, fminf(fk + (float)(t + 1), hi) - fmaxf(fk + (float)t, lo));
-                int ntl = 1;
+                int ntl = 2;
 #pragma unroll
-                for (int t = 1; t < 4; ++t) ntl = (ov[t] > 0.0f) ? t + 1 : ntl;
-                PatchCells H;
-                H.base = &sm.buf[b][0][k0 - wcur.kb];
-                H.lb = wcur.lb;
-                H.nt = __reduce_max_sync(0xffffffffu, ntl);
-                H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
-                sweep_rows<kTR / 2>(H, Bj, A, tau, g, acc);
-                sweep_rows<kTR / 2>(H, Bj + kTR / 2, A, tau, g, acc + kTR / 2);
+                for (int t = 2; t < 4; ++t) ntl = (ov[t] > 0.0f) ? t + 1 : ntl;
+                const int nt = __reduce_max_sync(0xffffffffu, ntl);
+                const bool mid = __any_sync(0xffffffffu, rows_ext > 0.99f);
+                const float *patch = &sm.buf[b][0][k0 - wcur.kb];
+                if (nt == 2) {
+                    if (mid) sweep_tile<2, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    else sweep_tile<2, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                } else if (nt == 3) {
+                    if (mid) sweep_tile<3, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    else sweep_tile<3, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                } else {
+                    if (mid) sweep_tile<4, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    else sweep_tile<4, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                }
             } else {
                 // Cell-by-cell overlap from global memory; row values go through
                 // shared memory so the row loop stays rolled (small code).

@@ -23,7 +23,7 @@ namespace ctgb {
 struct FilterHeaderDev {
     int zpl, log2zpl, nu, nv;
     float R;
-    int pad[3];
+    int flip, pad[2];
     long long off_h, off_tw, off_kk, off_pp, total;
 };
 
@@ -47,12 +47,14 @@ fdk_filter_kernel(const float *__restrict__ F, float *__restrict__ proj, long lo
     float *rowb = proj + rb * nu;
     const float pa = pp[ra % nv], pb = has_b ? pp[rb % nv] : 0.0f;
     // Load weighted rows at bit-reversed positions (zero padding beyond nu).
+    const int flip = f.flip;
     for (int n = threadIdx.x; n < N; n += blockDim.x) {
         float2 z = make_float2(0.0f, 0.0f);
         if (n < nu) {
             const float k2 = kk[n] * kk[n];
-            z.x = rowa[n] * (R * rsqrtf(R * R + k2 + pa * pa));
-            if (has_b) z.y = rowb[n] * (R * rsqrtf(R * R + k2 + pb * pb));
+            const int src = flip ? nu - 1 - n : n;   // ConeBeamGPU.py:298 weights fliplr(proj)
+            z.x = rowa[src] * (R * rsqrtf(R * R + k2 + pa * pa));
+            if (has_b) z.y = rowb[src] * (R * rsqrtf(R * R + k2 + pb * pb));
         }
         sm[bitrev(n, bits)] = z;
     }
@@ -125,6 +127,25 @@ extern "C" int ctgb_fdk_filter(const ctgb_params *p, const void *d_filter, float
     }
     fdk_filter_kernel<<<(unsigned)nblocks, kFftThreads, smem, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const float *>(d_filter), d_proj, nrows);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_filter_apply(const void *d_filter, int32_t zpl, float *d_rows, int64_t nrows, void *stream) {
+    clear_error();
+    if (!d_filter || !d_rows || nrows < 0 || zpl < 2 || zpl > 8192 || (zpl & (zpl - 1)))
+        return set_error(CTGB_ERR_ARG, "ctgb_filter_apply: bad arguments");
+    if (nrows == 0) return CTGB_OK;
+    const long long nblocks = (nrows + 1) / 2;
+    if (nblocks > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "ctgb_filter_apply: too many rows");
+    const size_t smem = (size_t)zpl * sizeof(float2);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fdk_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter smem: %s", cudaGetErrorString(e));
+    }
+    fdk_filter_kernel<<<(unsigned)nblocks, kFftThreads, smem, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float *>(d_filter), d_rows, nrows);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;

@@ -195,7 +195,7 @@ namespace ctgb {
 struct FilterHeader {
     int32_t zpl, log2zpl, nu, nv;
     float R;
-    int32_t pad[3];
+    int32_t flip, pad[2];
     int64_t off_h, off_tw, off_kk, off_pp, total;
 };
 
@@ -226,7 +226,12 @@ static FilterHeader filter_layout(const ctgb_params *p) {
 // Filter(N, pixel_size, FilterType, cutoff) restated (Reconstruction_numba.py:190-225):
 // spatial Ram-Lak kernel h, |fftshift(fft(h))| by a direct float64 DFT of
 // length N-1, window, cutoff.  Returns the centred-order spectrum.
-static std::vector<double> ramp_spectrum(int N, double tau, int type, double cutoff) {
+//   variant 0: Reconstruction.Filter — cutoff |w| > pi*cutoff/(2*tau)
+//   variant 1: ConeBeam.Filter / FanBeam.Filter (python/ConeBeamGPU.py:353-379,
+//              python/FanBeam.py:175-209) — spectrum doubled, cutoff |w| > pi*cutoff
+//   variant 2: equiangular kernel of matlab/FilterArc.m (odd taps
+//              -1/(2 pi^2 tau^2 sin^2(n tau))), cutoff as variant 0
+static std::vector<double> ramp_spectrum(int N, double tau, int type, double cutoff, int variant = 0) {
     const int M = N - 1;
     std::vector<double> h(M), x(N);
     for (int i = 0; i < N; ++i) x[i] = i - (N - 1) / 2.0;
@@ -235,8 +240,14 @@ static std::vector<double> ramp_spectrum(int N, double tau, int type, double cut
         double m = std::fmod(xi, 2.0);
         if (m < 0) m += 2.0;   // numpy's % follows the divisor's sign
         if (xi == 0) h[i] = 1.0 / (8.0 * tau * tau);
-        else if (m == 1.0) h[i] = -0.5 / ((M_PI * tau * xi) * (M_PI * tau * xi));
-        else h[i] = 0.0;
+        else if (m == 1.0) {
+            if (variant == 2) {
+                const double sn = std::sin(xi * tau);
+                h[i] = -1.0 / (2.0 * M_PI * M_PI * tau * tau * sn * sn);
+            } else {
+                h[i] = -0.5 / ((M_PI * tau * xi) * (M_PI * tau * xi));
+            }
+        } else h[i] = 0.0;
     }
     // |DFT(h)| then fftshift.
     std::vector<double> mag(M);
@@ -252,7 +263,7 @@ static std::vector<double> ramp_spectrum(int N, double tau, int type, double cut
         mag[k] = (double)std::sqrt(re * re + im * im);
     }
     std::vector<double> filt(M);
-    for (int k = 0; k < M; ++k) filt[k] = mag[(k + M / 2) % M];   // fftshift (M even)
+    for (int k = 0; k < M; ++k) filt[k] = mag[(k + M / 2) % M] * (variant == 1 ? 2.0 : 1.0);   // fftshift (M even)
     for (int k = 0; k < M; ++k) {
         double w = 2 * M_PI * x[k] / (N - 1);
         double f = filt[k];
@@ -265,7 +276,8 @@ static std::vector<double> ramp_spectrum(int N, double tau, int type, double cut
             case 4: f *= (0.5 + 0.5 * std::cos(w / cutoff)); break;
             default: break;
         }
-        if (std::fabs(w) > M_PI * cutoff / (2.0 * tau)) f = 0;
+        const double lim = (variant == 1) ? M_PI * cutoff : M_PI * cutoff / (2.0 * tau);
+        if (std::fabs(w) > lim) f = 0;
         filt[k] = f;
     }
     return filt;
@@ -311,5 +323,82 @@ extern "C" int ctgb_filter_build(const ctgb_params *p, int32_t filter_type, doub
     for (int i = 0; i < p->nv; ++i)
         B[f.off_pp + i] = (float)(((i - p->nv / 2.0) * (pyc ? -p->dv : p->dv) + voff) * R / (R + D));
     std::memcpy(host_buf, &f, sizeof f);
+    return CTGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Standalone reconstructors' filter tables (ConeBeam / FanBeam).
+static bool sa_valid(const ctgb_conebeam_params *p) {
+    return p && p->source_to_axis > 0 && p->source_to_detector > p->source_to_axis && p->pixel_width > 0 &&
+           p->det_width >= 2 && p->det_height >= 1 && p->nviews >= 1;
+}
+
+static FilterHeader sa_layout(const ctgb_conebeam_params *p) {
+    ctgb_params q;
+    std::memset(&q, 0, sizeof q);
+    q.nu = p->det_width;
+    q.nv = p->det_height;
+    return filter_layout(&q);
+}
+
+extern "C" int ctgb_standalone_filter_bytes(const ctgb_conebeam_params *p, size_t *bytes) {
+    clear_error();
+    if (!sa_valid(p) || !bytes) return set_error(CTGB_ERR_ARG, "ctgb_standalone_filter_bytes: bad geometry");
+    FilterHeader f = sa_layout(p);
+    if (f.zpl > 8192) return set_error(CTGB_ERR_SIZE, "zero-padded row length above 8192");
+    *bytes = (size_t)f.total * sizeof(float);
+    return CTGB_OK;
+}
+
+// variant 0 cone beam (ConeBeamGPU.py:229-241, :298-302): weight R/sqrt(R^2+kk^2+pp^2)
+//   at iso-scaled pixel centres, rows flipped along u, no deltaS;
+// variant 1 fan line (FanBeam.py:111-122): weight R/sqrt(R^2+gamma^2), no deltaS;
+// variant 2 fan arc (matlab/FanBeamReconArc.m:13-27): weight D*dgamma*cos(gamma),
+//   arc kernel, gamma = channel angle (pitch pixel_width / SDD).
+extern "C" int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32_t variant, int32_t filter_type,
+                                            double cutoff, void *host_buf, size_t bytes) {
+    size_t need = 0;
+    int st = ctgb_standalone_filter_bytes(p, &need);
+    if (st) return st;
+    if (!host_buf || bytes < need) return set_error(CTGB_ERR_SIZE, "filter buffer too small");
+    if (filter_type < 0 || filter_type > 4) return set_error(CTGB_ERR_ARG, "unknown filter type");
+    if (variant < 0 || variant > 2) return set_error(CTGB_ERR_ARG, "unknown filter variant");
+    if (!(cutoff > 0)) return set_error(CTGB_ERR_ARG, "cutoff must be positive");
+    std::memset(host_buf, 0, need);
+    FilterHeader f = sa_layout(p);
+    const double R = p->source_to_axis, D = p->source_to_detector - R;
+    float *B = static_cast<float *>(host_buf);
+    const int nu = p->det_width, nv = p->det_height;
+    std::vector<double> filt;
+    double scale = 1.0;
+    if (variant == 2) {
+        const double dg = p->pixel_width / p->source_to_detector;   // channel angle
+        filt = ramp_spectrum(f.zpl + 1, dg, filter_type, cutoff, 2);
+        scale = R * dg;
+        f.R = (float)R;
+        for (int j = 0; j < nu; ++j) B[f.off_kk + j] = (float)(R * std::tan((j - (nu - 1) / 2.0) * dg));
+        for (int i = 0; i < nv; ++i) B[f.off_pp + i] = 0.0f;
+    } else {
+        const double tau = p->pixel_width * R / (R + D);
+        filt = ramp_spectrum(f.zpl + 1, tau, filter_type, cutoff, 1);
+        f.R = (float)R;
+        for (int j = 0; j < nu; ++j) B[f.off_kk + j] = (float)((j - (nu - 1) / 2.0) * tau);
+        for (int i = 0; i < nv; ++i)
+            B[f.off_pp + i] = variant == 0 ? (float)((i - (nv - 1) / 2.0) * p->pixel_height * R / (R + D)) : 0.0f;
+        f.flip = variant == 0 ? 1 : 0;
+    }
+    for (int k = 0; k < f.zpl; ++k) B[f.off_h + k] = (float)(filt[(k + f.zpl / 2) % f.zpl] * scale / f.zpl);
+    for (int k = 0; k < f.zpl / 2; ++k) {
+        B[f.off_tw + 2 * k] = (float)std::cos(2 * M_PI * k / f.zpl);
+        B[f.off_tw + 2 * k + 1] = (float)std::sin(2 * M_PI * k / f.zpl);
+    }
+    std::memcpy(host_buf, &f, sizeof f);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_filter_zpl(const void *host_buf, int32_t *zpl) {
+    clear_error();
+    if (!host_buf || !zpl) return set_error(CTGB_ERR_ARG, "ctgb_filter_zpl: NULL argument");
+    *zpl = static_cast<const FilterHeader *>(host_buf)->zpl;
     return CTGB_OK;
 }

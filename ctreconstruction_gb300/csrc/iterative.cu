@@ -1,0 +1,291 @@
+// Element-wise and stencil kernels of the iterative drivers.
+//
+// Each kernel restates one update line of the reference scripts in float32
+// (the reference works on float32 NumPy arrays):
+//   SART      python/SART.py:51,55
+//   MLEM      python/EM.py:36-42
+//   ASD-POCS  python/ASD_POCS.py:174-179 (POCS), :55-77 (tv_grad), :183,189 (norms)
+// All are HBM-bound streaming passes (grid-stride loops over 4-float
+// vectors where the arrays allow it).  Reductions are deterministic: each
+// block writes one double partial sum, and the consumer sums the partials in
+// a fixed order.
+#include <cuda_runtime.h>
+
+#include "../../include/ctgb.h"
+#include "status.h"
+
+namespace ctgb {
+
+constexpr int kEwThreads = 256;
+
+static int ew_blocks(long long n) {
+    long long b = (n + kEwThreads * 4 - 1) / (kEwThreads * 4);
+    if (b < 1) b = 1;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)b;
+}
+
+// SART.py:51  r = (Ax - p0) / (A1 + eps)
+__global__ void sart_residual_kernel(const float *__restrict__ ax, const float *__restrict__ p0,
+                                     const float *__restrict__ a1, float eps, float *__restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (ax[i] - p0[i]) / (a1[i] + eps);
+}
+
+// SART.py:55  x = x_prev - alpha * (bp / norm1 + eps)   (eps added after the division, as written)
+__global__ void sart_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
+                                   const float *__restrict__ n1, float alpha, float eps, float *__restrict__ x,
+                                   long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = xp[i] - alpha * (bp[i] / n1[i] + eps);
+}
+
+// EM.py:36-39  p0[Ax == 0] = 0 (in place: the script's proj0 aliases the
+// measured data); Ax[Ax == 0] = eps; r = p0 / Ax
+__global__ void em_ratio_kernel(float *__restrict__ p0, const float *__restrict__ ax, float eps,
+                                float *__restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float a = ax[i], p = p0[i];
+        if (a == 0.0f) { p = 0.0f; p0[i] = 0.0f; a = eps; }
+        out[i] = p / a;
+    }
+}
+
+// EM.py:41-42  x = x_prev * (bp / norm)
+__global__ void em_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
+                                 const float *__restrict__ nrm, float *__restrict__ x, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = xp[i] * (bp[i] / nrm[i]);
+}
+
+// ASD_POCS.py:174-175  r = (p0 - Ax) / (A1 + eps); r[A1 == 0] = 0
+__global__ void pocs_residual_kernel(const float *__restrict__ p0, const float *__restrict__ ax,
+                                     const float *__restrict__ a1, float eps, float *__restrict__ out, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float d = a1[i];
+        out[i] = (d == 0.0f) ? 0.0f : (p0[i] - ax[i]) / (d + eps);
+    }
+}
+
+// ASD_POCS.py:177-179  bp[norm1 == 0] = 0; x = x_prev + beta * bp / (norm1 + eps); x[x < 0] = 0
+__global__ void pocs_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
+                                   const float *__restrict__ n1, float beta, float eps, float *__restrict__ x,
+                                   long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float d = n1[i];
+        const float b = (d == 0.0f) ? 0.0f : bp[i];
+        const float v = xp[i] + beta * b / (d + eps);
+        x[i] = v < 0.0f ? 0.0f : v;
+    }
+}
+
+// tv_grad (ASD_POCS.py:55-77) at interior voxel (i, j, k) of a [n0][n1][n2]
+// array: the sum of the four one-sided terms, before normalisation.
+__device__ __forceinline__ float tv_term(const float *__restrict__ x, int n1, int n2, int i, int j, int k, float eps) {
+    const long long s0 = (long long)n1 * n2, s1 = n2;
+    const long long c = i * s0 + j * s1 + k;
+    const float v = x[c];
+    const float w1 = v - x[c - s0], w2 = v - x[c - s1], w3 = v - x[c - 1];
+    const float t1 = (w1 + w2 + w3) / sqrtf(eps + w1 * w1 + w2 * w2 + w3 * w3);
+    const float xi = x[c + s0];
+    const float w4 = xi - v, w5 = xi - x[c + s0 - s1], w6 = xi - x[c + s0 - 1];
+    const float t2 = -w4 / sqrtf(eps + w4 * w4 + w5 * w5 + w6 * w6);
+    const float xj = x[c + s1];
+    const float w7 = xj - x[c - s0 + s1], w8 = xj - v, w9 = xj - x[c + s1 - 1];
+    const float t3 = -w8 / sqrtf(eps + w7 * w7 + w8 * w8 + w9 * w9);
+    const float xk = x[c + 1];
+    const float w10 = xk - x[c - s0 + 1], w11 = xk - x[c - s1 + 1], w12 = xk - v;
+    const float t4 = -w12 / sqrtf(eps + w10 * w10 + w11 * w11 + w12 * w12);
+    return t1 + t2 + t3 + t4;
+}
+
+// Pass 1: per-block partial sums of dtv^2 over the interior.
+__global__ void tv_norm_kernel(const float *__restrict__ x, int n0, int n1, int n2, float eps,
+                               double *__restrict__ partials) {
+    __shared__ double red[kEwThreads / 32];
+    const long long m0 = n0 - 2, m1 = n1 - 2, m2 = n2 - 2, tot = m0 * m1 * m2;
+    double acc = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % m2) + 1, j = (int)((t / m2) % m1) + 1, i = (int)(t / (m1 * m2)) + 1;
+        const float d = tv_term(x, n1, n2, i, j, k, eps);
+        acc += (double)d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kEwThreads / 32; ++w) s += red[w];
+        partials[blockIdx.x] = s;
+    }
+}
+
+__device__ __forceinline__ double sum_partials(const double *__restrict__ partials, int np) {
+    double s = 0.0;
+    for (int b = 0; b < np; ++b) s += partials[b];
+    return s;
+}
+
+// Pass 2: y = x - step * dtv / ||dtv|| (||dtv|| -> 1 when below eps); the
+// border of y is x's border (tv_grad pads dtv with zeros).
+__global__ void tv_step_kernel(const float *__restrict__ x, float *__restrict__ y, int n0, int n1, int n2, float eps,
+                               const double *__restrict__ partials, int np, float step) {
+    __shared__ float s_inv;
+    if (threadIdx.x == 0) {
+        float nrm = (float)sqrt(sum_partials(partials, np));
+        if (fabsf(nrm) < eps) nrm = 1.0f;
+        s_inv = 1.0f / nrm;
+    }
+    __syncthreads();
+    const float inv = s_inv;
+    const long long tot = (long long)n0 * n1 * n2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t % n2), j = (int)((t / n2) % n1), i = (int)(t / ((long long)n1 * n2));
+        float v = x[t];
+        if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1)
+            v = v - step * (tv_term(x, n1, n2, i, j, k, eps) * inv);
+        y[t] = v;
+    }
+}
+
+// Per-block partial sums of (a - b)^2 (b may be NULL: sum of a^2).
+__global__ void sqdist_kernel(const float *__restrict__ a, const float *__restrict__ b, long long n,
+                              double *__restrict__ partials) {
+    __shared__ double red[kEwThreads / 32];
+    double acc = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float d = b ? a[i] - b[i] : a[i];
+        acc += (double)d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kEwThreads / 32; ++w) s += red[w];
+        partials[blockIdx.x] = s;
+    }
+}
+
+// out[0] = sum of partials (one thread).
+__global__ void sum_partials_kernel(const double *__restrict__ partials, int np, double *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) out[0] = sum_partials(partials, np);
+}
+
+}  // namespace ctgb
+
+using namespace ctgb;
+
+static int ew_check(const char *who, long long n, const void *a, const void *b) {
+    if (n < 0 || !a || !b) return set_error(CTGB_ERR_ARG, "%s: bad arguments", who);
+    return CTGB_OK;
+}
+
+static int launched(const char *who) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "%s: %s", who, cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+#define EW_LAUNCH(kernel, n, stream, ...)                                                                    \
+    kernel<<<ew_blocks(n), kEwThreads, 0, static_cast<cudaStream_t>(stream)>>>(__VA_ARGS__)
+
+extern "C" int ctgb_partials_count(int64_t n, int32_t *count) {
+    clear_error();
+    if (!count || n < 0) return set_error(CTGB_ERR_ARG, "ctgb_partials_count: bad arguments");
+    *count = ew_blocks(n);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_sart_residual(const float *ax, const float *p0, const float *a1, float eps, float *out, int64_t n,
+                                  void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_sart_residual", n, ax, out)) return st;
+    if (!p0 || !a1) return set_error(CTGB_ERR_ARG, "ctgb_sart_residual: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(sart_residual_kernel, n, stream, ax, p0, a1, eps, out, n);
+    return launched("ctgb_sart_residual");
+}
+
+extern "C" int ctgb_sart_update(const float *x_prev, const float *bp, const float *norm1, float alpha, float eps,
+                                float *x, int64_t n, void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_sart_update", n, x_prev, x)) return st;
+    if (!bp || !norm1) return set_error(CTGB_ERR_ARG, "ctgb_sart_update: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(sart_update_kernel, n, stream, x_prev, bp, norm1, alpha, eps, x, n);
+    return launched("ctgb_sart_update");
+}
+
+extern "C" int ctgb_em_ratio(float *p0, const float *ax, float eps, float *out, int64_t n, void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_em_ratio", n, p0, ax)) return st;
+    if (!out) return set_error(CTGB_ERR_ARG, "ctgb_em_ratio: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(em_ratio_kernel, n, stream, p0, ax, eps, out, n);
+    return launched("ctgb_em_ratio");
+}
+
+extern "C" int ctgb_em_update(const float *x_prev, const float *bp, const float *norm, float *x, int64_t n,
+                              void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_em_update", n, x_prev, x)) return st;
+    if (!bp || !norm) return set_error(CTGB_ERR_ARG, "ctgb_em_update: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(em_update_kernel, n, stream, x_prev, bp, norm, x, n);
+    return launched("ctgb_em_update");
+}
+
+extern "C" int ctgb_pocs_residual(const float *p0, const float *ax, const float *a1, float eps, float *out,
+                                  int64_t n, void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_pocs_residual", n, p0, out)) return st;
+    if (!ax || !a1) return set_error(CTGB_ERR_ARG, "ctgb_pocs_residual: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(pocs_residual_kernel, n, stream, p0, ax, a1, eps, out, n);
+    return launched("ctgb_pocs_residual");
+}
+
+extern "C" int ctgb_pocs_update(const float *x_prev, const float *bp, const float *norm1, float beta, float eps,
+                                float *x, int64_t n, void *stream) {
+    clear_error();
+    if (int st = ew_check("ctgb_pocs_update", n, x_prev, x)) return st;
+    if (!bp || !norm1) return set_error(CTGB_ERR_ARG, "ctgb_pocs_update: NULL argument");
+    if (n == 0) return CTGB_OK;
+    EW_LAUNCH(pocs_update_kernel, n, stream, x_prev, bp, norm1, beta, eps, x, n);
+    return launched("ctgb_pocs_update");
+}
+
+extern "C" int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, int32_t n2, float eps, float step,
+                            double *partials, void *stream) {
+    clear_error();
+    if (!x || !y || !partials || n0 < 1 || n1 < 1 || n2 < 1 || x == y)
+        return set_error(CTGB_ERR_ARG, "ctgb_tv_step: bad arguments (x and y must differ)");
+    const long long tot = (long long)n0 * n1 * n2;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = ew_blocks(tot);
+    if (n0 < 3 || n1 < 3 || n2 < 3) {
+        cudaError_t e = cudaMemcpyAsync(y, x, sizeof(float) * tot, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "ctgb_tv_step: %s", cudaGetErrorString(e));
+        return CTGB_OK;
+    }
+    tv_norm_kernel<<<nb, kEwThreads, 0, st>>>(x, n0, n1, n2, eps, partials);
+    tv_step_kernel<<<nb, kEwThreads, 0, st>>>(x, y, n0, n1, n2, eps, partials, nb, step);
+    return launched("ctgb_tv_step");
+}
+
+extern "C" int ctgb_sqdist(const float *a, const float *b, int64_t n, double *partials, double *out, void *stream) {
+    clear_error();
+    if (!a || !partials || !out || n < 0) return set_error(CTGB_ERR_ARG, "ctgb_sqdist: bad arguments");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = ew_blocks(n);
+    sqdist_kernel<<<nb, kEwThreads, 0, st>>>(a, b, n, partials);
+    sum_partials_kernel<<<1, 32, 0, st>>>(partials, nb, out);
+    return launched("ctgb_sqdist");
+}

@@ -1,0 +1,224 @@
+"""Iterative reconstruction drivers on the GB300 projectors.
+
+Each driver restates one of the reference's scripts, with the same parameters
+and the same update formulas (including where the reference places eps):
+
+* ``sart``      python/SART.py:27-59   (all views per update, SIRT-like)
+* ``mlem``      python/EM.py:20-44
+* ``asd_pocs``  python/ASD_POCS.py:137-201 (POCS + TV descent, adaptive steps)
+* ``os_sart``   ordered subsets of views (no reference counterpart)
+
+The scripts call ``Reconstruction.forward()``/``backward()``; here those are
+the device projectors (``Projector.forward`` / ``Projector.backproject_fdk``,
+which is the reference's FDK-weighted backward()).  ``matched=True`` uses the
+exact adjoint instead.  All arithmetic runs in libctgb kernels on device
+tensors; the host only reads back the scalars the scripts branch on.
+"""
+import ctypes
+import math
+
+import torch
+
+from . import _lib
+from .geometry import ReconstructionParams
+from .projector import Projector, _ptr, _stream
+
+
+def _n(t):
+    return int(t.numel())
+
+
+class _Scratch:
+    """Device work arrays of one driver run (allocated once, through torch)."""
+
+    def __init__(self, P, device):
+        self.P = P
+        vshape, pshape = P.volume_shape, P.proj_shape()
+        self.proj = torch.empty(pshape, dtype=torch.float32, device=device)
+        self.res = torch.empty(pshape, dtype=torch.float32, device=device)
+        self.bp = torch.empty(vshape, dtype=torch.float32, device=device)
+        cnt = ctypes.c_int32(0)
+        _lib.call("ctgb_partials_count", max(_n(self.bp), _n(self.proj)), ctypes.byref(cnt))
+        self.partials = torch.empty(cnt.value, dtype=torch.float64, device=device)
+        self.scalar = torch.empty(1, dtype=torch.float64, device=device)
+
+
+def _sqdist(S, a, b=None):
+    _lib.call("ctgb_sqdist", _ptr(a), _ptr(b) if b is not None else None, _n(a), _ptr(S.partials), _ptr(S.scalar),
+              _stream())
+    return S.scalar
+
+
+def _backproject(P, proj, out, matched):
+    if matched:
+        return P.backproject_matched(proj, out=out)
+    return P.backproject_fdk(proj, out=out)
+
+
+def _rmse(S, x, phantom):
+    return math.sqrt(_sqdist(S, x, phantom).item() / _n(x))
+
+
+def normalisers(P, matched=False):
+    """norm1 = backward(ones) (SART.py:31-35), norm2 = forward(ones) (:36-38)."""
+    dev = P.device
+    ones_p = torch.ones(P.proj_shape(), dtype=torch.float32, device=dev)
+    norm1 = _backproject(P, ones_p, None, matched)
+    norm2 = P.forward(torch.ones(P.volume_shape, dtype=torch.float32, device=dev))
+    return norm1, norm2
+
+
+def sart(P, proj0, niter=10, alpha=1.0, eps=1e-5, x0=None, phantom=None, matched=False, norms=None):
+    """SART.py:44-59: x <- x - alpha * (B((Ax - p0) / (A1 + eps)) / norm1 + eps).
+
+    Returns (x, rmse list).  x0 defaults to zeros, as in the script."""
+    P = P if isinstance(P, Projector) else Projector(P)
+    dev = P.device
+    S = _Scratch(P, dev)
+    norm1, norm2 = norms if norms is not None else normalisers(P, matched)
+    x = torch.zeros(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+    xn = torch.empty_like(x)
+    rmse = []
+    n_p, n_v = _n(S.proj), _n(x)
+    for _ in range(niter):
+        P.forward(x, out=S.proj)
+        _lib.call("ctgb_sart_residual", _ptr(S.proj), _ptr(proj0), _ptr(norm2), eps, _ptr(S.res), n_p, _stream())
+        _backproject(P, S.res, S.bp, matched)
+        _lib.call("ctgb_sart_update", _ptr(x), _ptr(S.bp), _ptr(norm1), alpha, eps, _ptr(xn), n_v, _stream())
+        x, xn = xn, x
+        if phantom is not None:
+            rmse.append(_rmse(S, x, phantom))
+    return x, rmse
+
+
+def mlem(P, proj0, niter=10, eps=1e-5, x0=None, phantom=None, matched=False, norm=None):
+    """EM.py:32-44: x <- x * B(p0 / Ax) / B(1) with the script's zero guards.
+
+    proj0 is modified in place where Ax == 0 (the script's proj0 aliases its
+    measured data).  x0 defaults to ones, as in the script."""
+    P = P if isinstance(P, Projector) else Projector(P)
+    dev = P.device
+    S = _Scratch(P, dev)
+    if norm is None:
+        norm = _backproject(P, torch.ones(P.proj_shape(), dtype=torch.float32, device=dev), None, matched)
+    x = torch.ones(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+    xn = torch.empty_like(x)
+    rmse = []
+    n_p, n_v = _n(S.proj), _n(x)
+    for _ in range(niter):
+        P.forward(x, out=S.proj)
+        _lib.call("ctgb_em_ratio", _ptr(proj0), _ptr(S.proj), eps, _ptr(S.res), n_p, _stream())
+        _backproject(P, S.res, S.bp, matched)
+        _lib.call("ctgb_em_update", _ptr(x), _ptr(S.bp), _ptr(norm), _ptr(xn), n_v, _stream())
+        x, xn = xn, x
+        if phantom is not None:
+            rmse.append(_rmse(S, x, phantom))
+    return x, rmse
+
+
+def tv_descent(x, step, ng, eps=1e-7):
+    """ng steps of x <- x - step * tv_grad(x) (ASD_POCS.py:188-190; tv_grad
+    :55-77).  Returns a new tensor; x is not modified."""
+    nz, ny, nx = x.shape
+    cnt = ctypes.c_int32(0)
+    _lib.call("ctgb_partials_count", _n(x), ctypes.byref(cnt))
+    partials = torch.empty(cnt.value, dtype=torch.float64, device=x.device)
+    bufs = (torch.empty_like(x), torch.empty_like(x))
+    a = x
+    for i in range(ng):
+        out = bufs[i % 2]
+        _lib.call("ctgb_tv_step", _ptr(a), _ptr(out), nz, ny, nx, eps, float(step), _ptr(partials), _stream())
+        a = out
+    return a.clone() if ng == 0 else a
+
+
+def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.007, r_max=0.99, alpha_red=0.95,
+             eps=1e-7, x0=None, phantom=None, matched=False, norms=None, filter_type=None, cutoff=None):
+    """ASD_POCS.py:137-201.  x0 defaults to the script's FBP start
+    (Filtering() then backward() of proj0).  Returns (x, rmse list, log)."""
+    P = P if isinstance(P, Projector) else Projector(P)
+    dev = P.device
+    S = _Scratch(P, dev)
+    norm1, norm2 = norms if norms is not None else normalisers(P, matched)
+    if x0 is None:
+        q = proj0.clone()
+        P.filter(q, filter_type, cutoff)
+        x = P.backproject_fdk(q)
+    else:
+        x = x0.clone()
+    xn = torch.empty_like(x)
+    f0 = torch.empty_like(x)
+    tv_a, tv_b = torch.empty_like(x), torch.empty_like(x)
+    n_p, n_v = _n(S.proj), _n(x)
+    rmse, log = [], []
+    nz, ny, nx = x.shape
+    for _ in range(niter):
+        f0.copy_(x)
+        for _a in range(na):
+            P.forward(x, out=S.proj)
+            _lib.call("ctgb_pocs_residual", _ptr(proj0), _ptr(S.proj), _ptr(norm2), eps, _ptr(S.res), n_p, _stream())
+            _backproject(P, S.res, S.bp, matched)
+            _lib.call("ctgb_pocs_update", _ptr(x), _ptr(S.bp), _ptr(norm1), beta, eps, _ptr(xn), n_v, _stream())
+            x, xn = xn, x
+        dp = math.sqrt(_sqdist(S, x, f0).item())
+        dtvg = alpha * dp
+        f0.copy_(x)
+        a, b = x, tv_a
+        for _g in range(ng):
+            _lib.call("ctgb_tv_step", _ptr(a), _ptr(b), nz, ny, nx, eps, float(dtvg), _ptr(S.partials), _stream())
+            a, b = b, (tv_b if b is tv_a else tv_a)
+        if a is not x:
+            x.copy_(a)
+        dg = math.sqrt(_sqdist(S, x, f0).item())
+        if dg > r_max * dp:
+            alpha *= alpha_red
+        beta *= beta_red
+        log.append({"dtvg": dtvg, "beta": beta, "dp": dp, "dg": dg, "alpha": alpha})
+        if phantom is not None:
+            rmse.append(_rmse(S, x, phantom))
+    return x, rmse, log
+
+
+def os_sart(P, proj0, nsubsets=10, niter=20, lam=0.8, eps=1e-5, x0=None, phantom=None, matched=True):
+    """Ordered-subsets SART (no reference counterpart).
+
+    Subset s holds views s, s + nsubsets, s + 2 nsubsets, ... — itself a
+    regular scan (StartAngle + s * dtheta, the same angular span,
+    NumberOfViews / nsubsets views), so each subset gets its own Projector.
+    Each sub-iteration applies
+        x <- max(0, x + lam * B_s((p0_s - A_s x) / (A_s 1 + eps)) / (B_s 1 + eps))
+    with rows/voxels whose normaliser is zero left untouched."""
+    P = P if isinstance(P, Projector) else Projector(P)
+    dev = P.device
+    base = P.params
+    nv = base.NumberOfViews
+    if nsubsets < 1 or nv % nsubsets:
+        raise ValueError("NumberOfViews (%d) must be divisible by nsubsets (%d)" % (nv, nsubsets))
+    span = base.EndAngle - base.StartAngle
+    step = span / nv
+    vol_ones = torch.ones(P.volume_shape, dtype=torch.float32, device=dev)
+    subsets = []
+    for s in range(nsubsets):
+        d = base.as_dict()
+        d['StartAngle'] = base.StartAngle + s * step
+        d['EndAngle'] = d['StartAngle'] + span
+        d['NumberOfViews'] = nv // nsubsets
+        Ps = Projector(ReconstructionParams.from_dict(d, base.flavour), device=dev)
+        ps0 = proj0[s::nsubsets].contiguous()
+        a1 = Ps.forward(vol_ones)
+        b1 = _backproject(Ps, torch.ones_like(ps0), None, matched)
+        subsets.append((Ps, ps0, a1, b1))
+    x = torch.zeros(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+    S = _Scratch(subsets[0][0], dev)
+    n_v = _n(x)
+    rmse = []
+    for _ in range(niter):
+        for Ps, ps0, a1, b1 in subsets:
+            Ps.forward(x, out=S.proj)
+            _lib.call("ctgb_pocs_residual", _ptr(ps0), _ptr(S.proj), _ptr(a1), eps, _ptr(S.res), _n(S.res),
+                      _stream())
+            _backproject(Ps, S.res, S.bp, matched)
+            _lib.call("ctgb_pocs_update", _ptr(x), _ptr(S.bp), _ptr(b1), lam, eps, _ptr(x), n_v, _stream())
+        if phantom is not None:
+            rmse.append(_rmse(S, x, phantom))
+    return x, rmse

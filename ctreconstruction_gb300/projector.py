@@ -37,6 +37,7 @@ class Projector:
         self.table = torch.from_numpy(host).to(self.device)
         self._filters = {}
         self._xzy = None
+        self._ws = None
 
     # -- helpers --------------------------------------------------------------
     def _check(self, t, shape, name):
@@ -95,9 +96,29 @@ class Projector:
             accumulate = False
         self._check(out, self.volume_shape, "out")
         sc = self.params.dtheta if scale is None else float(scale)
-        _lib.call("ctgb_backproject_fdk", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out), view0,
-                  nviews, sc, int(bool(accumulate)), _stream())
+        ws = self._workspace(nviews)
+        if ws is None:
+            _lib.call("ctgb_backproject_fdk", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out), view0,
+                      nviews, sc, int(bool(accumulate)), _stream())
+        else:
+            _lib.call("ctgb_backproject_fdk_ws", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out),
+                      view0, nviews, sc, int(bool(accumulate)), _ptr(ws), ws.numel() * 4, _stream())
         return out
+
+    # Integrated-projection workspace of the FDK backprojector: all views when
+    # that fits in WORKSPACE_CAP bytes, else chunks of views.
+    WORKSPACE_CAP = 6 << 30
+
+    def _workspace(self, nviews):
+        if nviews == 0 or self.params.nu < 4:
+            return None
+        n = ctypes.c_size_t(0)
+        _lib.call("ctgb_backproject_fdk_workspace_bytes", ctypes.byref(self.c), 1, ctypes.byref(n))
+        per_view = n.value
+        want = min(nviews * per_view, max(per_view, self.WORKSPACE_CAP // per_view * per_view))
+        if self._ws is None or self._ws.numel() * 4 < want:
+            self._ws = torch.empty((want + 3) // 4, dtype=torch.float32, device=self.device)
+        return self._ws
 
     def backproject_matched(self, proj, out=None, view0=0, nviews=None, scale=1.0, accumulate=False):
         """vol = scale * A^T proj (exact adjoint of forward)."""

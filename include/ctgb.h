@@ -97,6 +97,17 @@ int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t 
 int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                          int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
 
+/* Same result as ctgb_backproject_fdk, faster: the projections are first
+ * integrated along v into a caller-supplied workspace of float2 (running sum,
+ * value) per detector cell and view, so each voxel's footprint costs two
+ * lookups per detector column.  Views are processed in chunks that fit the
+ * workspace (at least one view: ctgb_backproject_fdk_workspace_bytes(p, 1, ..)).
+ * Replaces the same reference code as ctgb_backproject_fdk. */
+int ctgb_backproject_fdk_workspace_bytes(const ctgb_params *p, int32_t nviews, size_t *bytes);
+int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                            int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
+                            size_t workspace_bytes, void *stream);
+
 /* ---- matched DD backprojection (exact adjoint of ctgb_forward) -------------
  * No reference counterpart (the reference's backward() is FDK-weighted);
  * vol = (accumulate ? vol : 0) + scale * A^T proj. */
@@ -114,6 +125,73 @@ int ctgb_backproject_matched(const ctgb_params *p, const void *d_table, const fl
 int ctgb_filter_bytes(const ctgb_params *p, size_t *bytes);
 int ctgb_filter_build(const ctgb_params *p, int32_t filter_type, double cutoff, void *host_buf, size_t bytes);
 int ctgb_fdk_filter(const ctgb_params *p, const void *d_filter, float *d_proj, int32_t nviews, void *stream);
+
+/* ---- standalone cone-beam and fan-beam reconstructors ------------------------
+ * Geometry of python/ConeBeam.py / ConeBeamGPU.py / FanBeam.py, read there from
+ * a "key: value" text file (ReconstructionParams.txt, ConeBeam.py:57-84):
+ * SourceToAxis, SourceToDetector, DetectorPixelWidth/Height,
+ * DetectorWidth/Height (columns/rows), NumberOfViews, AngleCoverage (here in
+ * radians), ReconVolume X*Y*Z.  For fan beam, DetectorHeight is the number of
+ * slices and recon_z must equal it. */
+typedef struct ctgb_conebeam_params {
+    double source_to_axis, source_to_detector;
+    double pixel_width, pixel_height;
+    int32_t det_width, det_height;
+    int32_t nviews;
+    double angle_coverage;
+    int32_t recon_x, recon_y, recon_z;
+    int32_t arc;                    /* fan beam: 1 equiangular arc detector, 0 equispaced line */
+} ctgb_conebeam_params;
+
+/* Voxel-driven weighted FDK backprojection; replaces ConeBeamGPU.Reconstruction's
+ * per-view CalculateInterpolGrid + Interpol2dLineargpu launches
+ * (python/ConeBeamGPU.py:296-313; python/GPUFuncs_pycuda.py:40-102).
+ * q: filtered projections [nviews][det_height][det_width]; recon: [Z][Y][X]. */
+int ctgb_conebeam_table_bytes(const ctgb_conebeam_params *p, size_t *bytes);
+int ctgb_conebeam_table_build(const ctgb_conebeam_params *p, void *host_table, size_t bytes);
+int ctgb_conebeam_backproject(const ctgb_conebeam_params *p, const void *d_table, const float *d_q, float *d_recon,
+                              int32_t view0, int32_t nviews, int32_t accumulate, void *stream);
+
+/* Filter tables of the standalone reconstructors (ConeBeam.Filter / FanBeam.Filter,
+ * python/ConeBeamGPU.py:353-379, python/FanBeam.py:175-209; arc kernel
+ * matlab/FilterArc.m): variant 0 cone beam (cosine weight over u and v, rows
+ * flipped along u as ConeBeamGPU.py:298 does), 1 fan line, 2 fan arc.  Same
+ * layout as ctgb_filter_build; apply with ctgb_filter_apply. */
+int ctgb_standalone_filter_bytes(const ctgb_conebeam_params *p, size_t *bytes);
+int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32_t variant, int32_t filter_type, double cutoff,
+                                 void *host_buf, size_t bytes);
+/* Filter nrows rows of length nu in place with a table from ctgb_filter_build
+ * or ctgb_standalone_filter_build (rows grouped by nv rows per view for the
+ * cosine weight). */
+int ctgb_filter_apply(const void *d_filter, int32_t zpl, float *d_rows, int64_t nrows, void *stream);
+/* zpl (zero-padded row length) of a host filter table. */
+int ctgb_filter_zpl(const void *host_buf, int32_t *zpl);
+
+/* ---- batched 2-D fan-beam backprojection -------------------------------------
+ * Many fan-beam slices of uneven image size in one persistent launch (the
+ * per-slice backprojection of python/FanBeam.py:110-131, line detector, or
+ * matlab/FanBeamReconArc.m:34-47, arc detector).  Each slice has its own
+ * image grid, scan geometry and filtered sinogram [nviews][nch]; the work list
+ * is (slice, tile) items of tile_x x tile_y pixels. */
+typedef struct ctgb_fan_slice {
+    int32_t nx, ny;            /* image columns / rows; the image is [ny][nx] */
+    float x0, dx, y0, dy;      /* pixel centres x = x0 + i*dx, y = y0 + j*dy (mm) */
+    float R, D;                /* source-to-axis; line: SourceToDetector - R (the U weight) */
+    float g0, dg;              /* detector samples: line iso-scaled positions (mm), arc angles (rad) */
+    int32_t nch, nviews;
+    float theta0, dtheta;      /* view angles theta0 + v*dtheta; dtheta also scales the sum */
+    int32_t arc, pad;
+    int64_t sino_offset;       /* floats from the sinogram base */
+    int64_t image_offset;      /* floats from the image base */
+} ctgb_fan_slice;
+
+int ctgb_fan_batch_bytes(const ctgb_fan_slice *slices, int32_t nslices, int32_t tile_x, int32_t tile_y, size_t *bytes);
+int ctgb_fan_batch_build(const ctgb_fan_slice *slices, int32_t nslices, int32_t tile_x, int32_t tile_y,
+                         void *host_buf, size_t bytes);
+/* images[slice] (+)= backprojection; grid_blocks persistent CTAs of tile_x*tile_y
+ * threads (the tile the batch was built with); max_views >= every slice's nviews. */
+int ctgb_fan_backproject(const void *d_batch, int32_t max_views, const float *d_sino, float *d_images,
+                         int32_t tile_x, int32_t tile_y, int32_t grid_blocks, int32_t accumulate, void *stream);
 
 /* ---- status ----------------------------------------------------------------
  * ctgb_device_status: the device-side status word of the current device

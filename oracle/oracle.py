@@ -189,3 +189,90 @@ def fdk_filter(proj, nu, nv, du, dv, sad, sdd, filter_type, cutoff, offset=(0, 0
     spec = np.fft.fftshift(np.fft.fft(wp, zpl, axis=-1), axes=-1)
     q = np.real(np.fft.ifft(np.fft.ifftshift(filt * spec, axes=-1), axis=-1))[..., :nu]
     return q * delta_s
+
+
+# -- iterative drivers (python/SART.py, python/EM.py, python/ASD_POCS.py) -------
+def sart(g, proj0, niter, alpha=1.0, eps=1e-5, x0=None):
+    """SART.py:27-59 in float32 NumPy over the oracle projectors."""
+    f32 = np.float32
+    norm1 = g.backward_fdk(np.ones((g.nviews, g.nv, g.nu), np.float32)).astype(f32)
+    norm2 = g.forward(np.ones((g.nz, g.ny, g.nx), np.float32)).astype(f32)
+    x = np.zeros((g.nz, g.ny, g.nx), f32) if x0 is None else x0.astype(f32).copy()
+    for _ in range(niter):
+        p = g.forward(x).astype(f32)
+        r = (p - proj0) / (norm2 + f32(eps))
+        b = g.backward_fdk(r.astype(f32)).astype(f32)
+        x = x - f32(alpha) * (b / norm1 + f32(eps))
+    return x
+
+
+def mlem(g, proj0, niter, eps=1e-5, x0=None):
+    """EM.py:20-44 (proj0 is modified where the forward projection is zero)."""
+    f32 = np.float32
+    norm = g.backward_fdk(np.ones((g.nviews, g.nv, g.nu), np.float32)).astype(f32)
+    x = np.ones((g.nz, g.ny, g.nx), f32) if x0 is None else x0.astype(f32).copy()
+    for _ in range(niter):
+        p = g.forward(x).astype(f32)
+        proj0[p == 0] = 0
+        p[p == 0] = f32(eps)
+        r = proj0 / p
+        b = g.backward_fdk(r.astype(f32)).astype(f32)
+        x = x * (b / norm)
+    return x
+
+
+def tv_grad(image, eps=1e-7):
+    """ASD_POCS.py:55-77 (np.lib.pad replaced by np.pad)."""
+    f32 = np.float32
+    e = f32(eps)
+    x = image
+    c = x[1:-1, 1:-1, 1:-1]
+    w1 = c - x[0:-2, 1:-1, 1:-1]; w2 = c - x[1:-1, 0:-2, 1:-1]; w3 = c - x[1:-1, 1:-1, 0:-2]
+    t1 = (w1 + w2 + w3) / np.sqrt(e + w1 ** 2 + w2 ** 2 + w3 ** 2)
+    w4 = x[2:, 1:-1, 1:-1] - c; w5 = x[2:, 1:-1, 1:-1] - x[2:, 0:-2, 1:-1]; w6 = x[2:, 1:-1, 1:-1] - x[2:, 1:-1, 0:-2]
+    t2 = (-w4) / np.sqrt(e + w4 ** 2 + w5 ** 2 + w6 ** 2)
+    w7 = x[1:-1, 2:, 1:-1] - x[0:-2, 2:, 1:-1]; w8 = x[1:-1, 2:, 1:-1] - c; w9 = x[1:-1, 2:, 1:-1] - x[1:-1, 2:, 0:-2]
+    t3 = (-w8) / np.sqrt(e + w7 ** 2 + w8 ** 2 + w9 ** 2)
+    w10 = x[1:-1, 1:-1, 2:] - x[0:-2, 1:-1, 2:]; w11 = x[1:-1, 1:-1, 2:] - x[1:-1, 0:-2, 2:]; w12 = x[1:-1, 1:-1, 2:] - c
+    t4 = (-w12) / np.sqrt(e + w10 ** 2 + w11 ** 2 + w12 ** 2)
+    dtv = t1 + t2 + t3 + t4
+    tv_norm = np.sqrt(np.sum(dtv.astype(np.float64) ** 2))
+    if abs(tv_norm) < eps:
+        tv_norm = 1.0
+    dtv = (dtv / f32(tv_norm)).astype(f32)
+    return np.pad(dtv, ((1, 1), (1, 1), (1, 1)), 'constant')
+
+
+def asd_pocs(g, proj0, niter, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.007, r_max=0.99, alpha_red=0.95,
+             eps=1e-7, x0=None):
+    """ASD_POCS.py:137-201; x0 defaults to Filtering() + backward() of proj0."""
+    f32 = np.float32
+    norm1 = g.backward_fdk(np.ones((g.nviews, g.nv, g.nu), np.float32)).astype(f32)
+    norm2 = g.forward(np.ones((g.nz, g.ny, g.nx), np.float32)).astype(f32)
+    if x0 is None:
+        x = g.backward_fdk(g.filtering(proj0).astype(f32)).astype(f32)
+    else:
+        x = x0.astype(f32).copy()
+    log = []
+    for _ in range(niter):
+        f0 = x.copy()
+        for _a in range(na):
+            tmp = x.copy()
+            p = g.forward(x).astype(f32)
+            r = (proj0 - p) / (norm2 + f32(eps))
+            r[norm2 == 0] = 0
+            b = g.backward_fdk(r.astype(f32)).astype(f32)
+            b[norm1 == 0] = 0
+            x = tmp + f32(beta) * b / (norm1 + f32(eps))
+            x[x < 0] = 0
+        dp = float(np.sqrt(np.sum((x.astype(np.float64) - f0) ** 2)))
+        dtvg = alpha * dp
+        f0 = x.copy()
+        for _g in range(ng):
+            x = (x - f32(dtvg) * tv_grad(x, eps)).astype(f32)
+        dg = float(np.sqrt(np.sum((x.astype(np.float64) - f0) ** 2)))
+        if dg > r_max * dp:
+            alpha *= alpha_red
+        beta *= beta_red
+        log.append({"dtvg": dtvg, "beta": beta, "dp": dp, "dg": dg, "alpha": alpha})
+    return x, log

@@ -18,16 +18,22 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
 
 
+def _dd_golden_files():
+    """Golden vectors of the DD path (Reconstruction_numba / _pycuda)."""
+    return [f for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+            if os.path.basename(f).startswith(("numba_", "pycuda_"))]
+
+
 def golden_cases():
     out = []
-    for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+    for f in _dd_golden_files():
         d = np.load(f)
         out.append((os.path.basename(f)[:-4], json.loads(str(d["params"])), str(d["flavour"]), d))
     return out
 
 
 def golden_ids():
-    return [os.path.basename(f)[:-4] for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))]
+    return [os.path.basename(f)[:-4] for f in _dd_golden_files()]
 
 
 def load_golden(name):

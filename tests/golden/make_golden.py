@@ -97,6 +97,69 @@ def run_case(Recon, p, image, proj, what):
     return out
 
 
+def conebeam_golden(ref_root, lib_path):
+    """python/ConeBeamGPU.py's reconstruction on a small case: the filter
+    spectrum from the reference's ConeBeam.Filter (ConeBeam.py parses; the
+    GPU file does not under Python 3), its filtering loop (ConeBeamGPU.py:
+    296-302) and, for the backprojection, the reference's own kernels
+    CalculateInterpolGrid + Interpol2dLineargpu run through oracle/_ref."""
+    import ctypes
+    import ConeBeam as CB
+    import FanBeam as FB
+    p = {'SourceToAxis': 100.0, 'SourceToDetector': 150.0, 'DetectorPixelWidth': 1.1, 'DetectorPixelHeight': 1.2,
+         'DetectorWidth': 24, 'DetectorHeight': 16, 'NumberOfViews': 12, 'AngleCoverage': 2 * PI,
+         'ReconX': 16, 'ReconY': 16, 'ReconZ': 8}
+    R, D = p['SourceToAxis'], p['SourceToDetector'] - p['SourceToAxis']
+    nx, ny, ns = p['DetectorWidth'], p['DetectorHeight'], p['NumberOfViews']
+    X, Y, Z = p['ReconX'], p['ReconY'], p['ReconZ']
+    rng = np.random.default_rng(300)
+    proj = rng.random((ny, nx, ns)).astype(np.float32)             # reference layout: views last
+    zpl = int(2 ** np.ceil(np.log2(2 * (nx - 1))))
+    filt = CB.ConeBeam.Filter(zpl + 1, p['DetectorPixelWidth'] * R / (D + R), 'ram-lak', 0.3)
+    fov = 2 * R * np.sin(np.arctan(nx * p['DetectorPixelWidth'] / 2 / (D + R)))
+    fovz = 2 * R * np.sin(np.arctan(ny * p['DetectorPixelHeight'] / 2 / (D + R)))
+    x = np.linspace(-fov / 2, fov / 2, X); y = np.linspace(-fov / 2, fov / 2, Y); z = np.linspace(-fovz / 2, fovz / 2, Z)
+    xx, yy = np.meshgrid(x, y)
+    ang = np.linspace(0, p['AngleCoverage'], ns + 1)[:-1]
+    dtheta = ang[1] - ang[0]
+    ki = (np.arange(0, nx) - (nx - 1) / 2) * p['DetectorPixelWidth'] * R / (R + D)
+    pp = (np.arange(0, ny) - (ny - 1) / 2) * p['DetectorPixelHeight'] * R / (R + D)
+    kk, ppm = np.meshgrid(ki, pp)
+    weight = R / np.sqrt(R ** 2 + kk ** 2 + ppm ** 2)
+    lib = ctypes.CDLL(lib_path)
+    fp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    pad = 64
+    ki_pad = np.zeros(nx + 2 * pad, np.float32); ki_pad[pad:pad + nx] = ki
+    pp_pad = np.zeros(ny + 2 * pad, np.float32); pp_pad[pad:pad + ny] = pp
+    dest = np.zeros(X * Y * Z, np.float32)
+    IX, IY, IW = (np.zeros(X * Y * Z, np.float32) for _ in range(3))
+    zz = z.astype(np.float32)
+    interp = np.array([ki.min(), ki[1] - ki[0], pp.min(), pp[1] - pp[0], nx, ny, X, Y, Z, 0, dtheta], np.float32)
+    gridp = np.array([R, X, Y, Z], np.float32)
+    Qs = np.zeros((ns, ny, nx), np.float32)
+    for i in range(ns):
+        wproj = weight * np.fliplr(proj[:, :, i])
+        Q = np.zeros(wproj.shape)
+        for k in range(ny):
+            tmp = np.real(np.fft.ifft(np.fft.ifftshift(filt * np.fft.fftshift(np.fft.fft(wproj[k, :], zpl)))))
+            Q[k, :] = tmp[0:nx]
+        Qs[i] = Q
+        t = (xx * np.cos(ang[i]) + yy * np.sin(ang[i])).flatten().astype(np.float32)
+        s_ = (-xx * np.sin(ang[i]) + yy * np.cos(ang[i])).flatten().astype(np.float32)
+        Qf = np.ascontiguousarray(Q.flatten().astype(np.float32))
+        lib.ref_fdk_interp_view(fp(dest), fp(Qf), ctypes.cast(ctypes.addressof(ki_pad.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_float)).contents) + 4 * pad, ctypes.POINTER(ctypes.c_float)),
+            ctypes.cast(ctypes.addressof(pp_pad.ctypes.data_as(ctypes.POINTER(ctypes.c_float)).contents) + 4 * pad,
+                        ctypes.POINTER(ctypes.c_float)),
+            fp(IX), fp(IY), fp(IW), fp(t), fp(s_), fp(zz), fp(gridp), fp(interp), 4)
+    fan = {}
+    for ft, co in (('hann', 0.3), ('ram-lak', 0.3), ('hamming', 0.5)):
+        fan['fan_filter_%s_%g' % (ft, co)] = FB.FanBeam.Filter(2049, 0.37, ft, co)
+    np.savez_compressed(os.path.join(HERE, "conebeam_ref.npz"), params=json.dumps(p), proj=proj,
+                        spectrum=filt, filtered=Qs, recon=dest.reshape(Z, Y, X), **fan)
+    print("conebeam_ref: recon range", float(dest.min()), float(dest.max()))
+
+
 def main(ref_root):
     sys.path.insert(0, os.path.join(ref_root, "python"))
     import _numba_stub
@@ -124,6 +187,8 @@ def main(ref_root):
         np.savez_compressed(os.path.join(HERE, name + ".npz"), params=json.dumps(p), flavour="numba",
                             image=image, proj=proj, **out, **extra)
         print("%s: %.1fs %s" % (name, time.time() - t0, sorted(list(out) + list(extra))))
+
+    conebeam_golden(ref_root, lib)
 
     for i, (name, p) in enumerate(PYCUDA_CASES):
         t0 = time.time()
