@@ -329,6 +329,197 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Other BASELINE configurations (one JSON line each; not the headline workload).
+def _timed(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def run_fdk128(args):
+    """FDK 128^3 (1 mm), 360 views, 256x192 detector (1.5 mm), SAD 1000, SDD
+    1500; modified Shepp-Logan, DD-forward projections with Poisson noise at
+    I0 = 1e5; Filtering() + backward() with a Hann ramp."""
+    import torch
+    from ctreconstruction_gb300 import Projector, phantoms
+    p = {'SourceInit': [0.0, 1000.0, 0.0], 'DetectorInit': [0.0, -500.0, 0.0], 'StartAngle': 0.0,
+         'EndAngle': 2 * np.pi, 'NumberOfDetectorPixels': [256, 192], 'DetectorPixelSize': [1.5, 1.5],
+         'NumberOfViews': 360, 'ImagePixelSpacing': [1.0, 1.0, 1.0], 'NumberOfImage': [128, 128, 128],
+         'FilterType': 'hann', 'cutoff': 1.0}
+    P = Projector(p)
+    ph = phantoms.shepp_logan_3d((128, 128, 128), device=P.device) * 0.02
+    clean = P.forward(ph)
+    gen = torch.Generator(device=P.device).manual_seed(0)
+    counts = torch.poisson(1e5 * torch.exp(-clean), generator=gen)
+    proj = -torch.log(torch.clamp(counts, min=1.0) / 1e5)
+    q = torch.empty_like(proj)
+    out = torch.empty(P.volume_shape, device=P.device)
+
+    def step():
+        q.copy_(proj)
+        P.filter(q)
+        P.backproject_fdk(q, out=out)
+
+    ms = _timed(step, args.steps, args.warmup)
+    vv = 128 ** 3 * 360
+    inner = ph.abs() > 0
+    rmse = float(torch.sqrt(torch.mean((out - ph)[inner] ** 2)))
+    return {"metric": "FDK reconstruction throughput", "value": vv / (ms / 1e3) / 1e9, "unit": UNIT,
+            "ms_per_step": ms, "higher_is_better": True, "dtype": "f32", "data": "synthetic (Shepp-Logan, Poisson)",
+            "config": {"workload": "fdk_128cube_360views_det256x192", "step": "Filtering() + backward()"},
+            "rmse_vs_phantom_inside": rmse}
+
+
+def run_fan_batch(args):
+    """256 fan-beam slices (86 x 256^2, 85 x 384^2, 85 x 512^2 on a 0.8 mm
+    grid), 720 views over 2 pi, 984 channels, SAD 570, SDD 1040 (line
+    detector pitch 1.0 mm; arc detector the same pitch as an arc length), 20
+    random ellipses per slice with exact line-integral sinograms.  One batch
+    = filtering (Hann, cutoff 1.0; the balanced equiangular kernel for the
+    arc detector) + one persistent backprojection launch with the autotuned
+    tile; both detector shapes are timed.  Quality: scale-fitted relative
+    error against the phantom on three slices."""
+    import torch
+    from ctreconstruction_gb300 import phantoms
+    from ctreconstruction_gb300.fanbeam import FanBatch, slice_from_grid
+    nviews, nch, sad, sdd, pitch = 720, 984, 570.0, 1040.0, 1.0
+    sizes = [256] * 86 + [384] * 85 + [512] * 85
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {}
+    rmse = {}
+    for arc in (False, True):
+        geom = type("G", (), dict(source_to_axis=sad, source_to_detector=sdd, pixel_width=pitch, det_width=nch,
+                                  nviews=nviews, angle_coverage=2 * np.pi))()
+        slices = [slice_from_grid(n, n, 0.8, geom, arc=arc) for n in sizes]
+        sinos, truth = [], []
+        for i, (n, s) in enumerate(zip(sizes, slices)):
+            half = (n - 1) / 2.0 * 0.8
+            ell = [(v, cx * half, cy * half, a * half, b * half, ph)
+                   for v, cx, cy, a, b, ph in phantoms.random_ellipses(20, seed=1000 + i)]
+            gam = s.g0 + s.dg * np.arange(nch)
+            sinos.append(phantoms.ellipse_fan_sinogram(ell, sad, nviews, gam, s.dtheta, arc=arc, device=dev))
+            if i in (0, 86, 171):
+                grid = torch.linspace(-half, half, n, device=dev)
+                truth.append((i, phantoms.ellipse_image(ell, grid, grid)))
+        batch = FanBatch(slices, filter_type='hann', cutoff=1.0, arc_kernel='balanced' if arc else 'reference')
+        flat = batch.pack(sinos)
+        work = torch.empty_like(flat)
+        images = torch.empty(batch.image_floats, device=flat.device)
+        work.copy_(flat)
+        batch.filter(work)
+        batch.backproject(work, images)            # autotunes the tile once (untimed)
+
+        def step():
+            work.copy_(flat)
+            batch.filter(work)
+            batch.backproject(work, images)
+
+        ms = _timed(step, args.steps, args.warmup)
+        imgs = batch.unpack(images)
+        errs = []
+        for i, t in truth:
+            k = float((imgs[i] * t).sum() / (t * t).sum())
+            errs.append(round(float(torch.linalg.norm(imgs[i] - k * t) / torch.linalg.norm(k * t)), 4))
+        rmse["arc" if arc else "line"] = errs
+        pv = sum(n * n for n in sizes) * nviews
+        out["arc" if arc else "line"] = {"ms_per_batch": ms, "Gpixel_views_per_s": pv / (ms / 1e3) / 1e9,
+                                         "tile": list(batch.tile), "fitted_rel_err_slices_0_86_171": rmse["arc" if arc else "line"]}
+    total_ms = out["line"]["ms_per_batch"] + out["arc"]["ms_per_batch"]
+    pv = sum(n * n for n in sizes) * nviews
+    return {"metric": "batched fan-beam FBP throughput", "value": 2 * pv / (total_ms / 1e3) / 1e9,
+            "unit": "Gpixel*views/s", "ms_per_step": total_ms, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (20 random ellipses per slice, exact line integrals)",
+            "config": {"workload": "fan_batch_256slices_720views_984ch", "detectors": ["line", "arc"]},
+            "detail": out}
+
+
+def run_iter(args):
+    """Batched OS-SART (10 subsets x 20 iterations, lambda 0.8) and MLEM (50
+    iterations) over 16 cone-beam scans, volumes 128^3..384^3 (multiples of
+    16), 90 views, detector 2N x 2N at 1.5x the voxel pitch, random ellipsoids
+    with Poisson noise at I0 = 5e4.  Times one OS-SART iteration (all scans,
+    all subsets) and one MLEM iteration (all scans)."""
+    import torch
+    from ctreconstruction_gb300 import Projector, iterative, phantoms
+    sides = [int(round(v / 16.0)) * 16 for v in np.linspace(128, 384, 16)]
+    scans = []
+    for i, n in enumerate(sides):
+        vox = 256.0 / n
+        p = {'SourceInit': [0.0, 1000.0, 0.0], 'DetectorInit': [0.0, -500.0, 0.0], 'StartAngle': 0.0,
+             'EndAngle': 2 * np.pi, 'NumberOfDetectorPixels': [2 * n, 2 * n],
+             'DetectorPixelSize': [1.5 * vox, 1.5 * vox], 'NumberOfViews': 90,
+             'ImagePixelSpacing': [vox, vox, vox], 'NumberOfImage': [n, n, n]}
+        P = Projector(p)
+        ph = phantoms.random_ellipsoids((n, n, n), n=30, seed=10 + i, device=P.device) * 0.01
+        clean = P.forward(ph)
+        gen = torch.Generator(device=P.device).manual_seed(i)
+        counts = torch.poisson(5e4 * torch.exp(-clean), generator=gen)
+        scans.append((P, -torch.log(torch.clamp(counts, min=1.0) / 5e4), ph))
+    t_os = t_em = 0.0
+    vv = 0
+    for P, proj, ph in scans:
+        x0 = torch.zeros(P.volume_shape, device=P.device)
+        iterative.os_sart(P, proj, nsubsets=10, niter=1, x0=x0)          # warm (workspaces, tables)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        iterative.os_sart(P, proj, nsubsets=10, niter=2, x0=x0)
+        b.record()
+        torch.cuda.synchronize()
+        t_os += a.elapsed_time(b) / 2
+        pc = proj.clone().clamp_(min=0)
+        iterative.mlem(P, pc, niter=1)
+        a.record()
+        iterative.mlem(P, pc, niter=2)
+        b.record()
+        torch.cuda.synchronize()
+        t_em += a.elapsed_time(b) / 2
+        vv += 2 * P.volume_shape[0] ** 3 * 90
+    return {"metric": "batched OS-SART / MLEM iteration throughput", "value": vv / ((t_os + t_em) / 2 / 1e3) / 1e9,
+            "unit": UNIT, "ms_per_step": (t_os + t_em) / 2, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (random ellipsoids, Poisson I0=5e4)",
+            "config": {"workload": "os_sart_mlem_16scans_128to384_90views", "sides": sides},
+            "os_sart_ms_per_iteration": t_os, "mlem_ms_per_iteration": t_em,
+            "os_sart_20_iterations_s": 20 * t_os / 1e3, "mlem_50_iterations_s": 50 * t_em / 1e3}
+
+
+def run_asd256(args):
+    """ASD-POCS at 256^3, 60 views, 512x384 detector (plain TV step, alpha
+    0.002, 20 TV steps, na = 5): time per outer iteration and RMSE."""
+    import torch
+    from ctreconstruction_gb300 import Projector, iterative, phantoms
+    p = {'SourceInit': [0.0, 1000.0, 0.0], 'DetectorInit': [0.0, -500.0, 0.0], 'StartAngle': 0.0,
+         'EndAngle': 2 * np.pi, 'NumberOfDetectorPixels': [512, 384], 'DetectorPixelSize': [0.75, 0.75],
+         'NumberOfViews': 60, 'ImagePixelSpacing': [0.5, 0.5, 0.5], 'NumberOfImage': [256, 256, 256],
+         'FilterType': 'hann', 'cutoff': 1.0}
+    P = Projector(p)
+    ph = phantoms.random_ellipsoids((256, 256, 256), n=30, seed=5, device=P.device) * 0.02
+    proj = P.forward(ph)
+    norms = iterative.normalisers(P)
+    iterative.asd_pocs(P, proj, niter=1, alpha=0.002, norms=norms)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    x, rmse, log = iterative.asd_pocs(P, proj, niter=3, alpha=0.002, norms=norms, phantom=ph)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / 3
+    return {"metric": "ASD-POCS outer-iteration time", "value": ms, "unit": "ms", "higher_is_better": False,
+            "dtype": "f32", "data": "synthetic (random ellipsoids)",
+            "config": {"workload": "asd_pocs_256cube_60views_det512x384", "na": 5, "ng": 20, "alpha": 0.002},
+            "rmse_per_iteration": rmse}
+
+
+WORKLOADS = {"fdk128": run_fdk128, "fan_batch": run_fan_batch, "iter": run_iter, "asd256": run_asd256}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,9 +529,19 @@ def main():
     ap.add_argument("--small", type=int, default=0, help="cube side for a quick small run (not the workload)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-matched", action="store_true")
+    ap.add_argument("--workload", default="dd512", choices=["dd512"] + sorted(WORKLOADS),
+                    help="dd512 (default) is the headline DD pair; the others time the remaining configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "dd512":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        line = WORKLOADS[args.workload](args)
+        line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
+                     "vs_baseline": None})
+        print(json.dumps(line))
+        return 0
     return run_ours(args)
 
 

@@ -261,19 +261,15 @@ __device__ __forceinline__ float integ_taps(const float2 *__restrict__ rlo, cons
     return s;
 }
 
-template <int NT, bool LINEAR>
+// CLAMP: some footprint of the chunk may leave the detector's rows [0, nv];
+// without it every footprint lies inside (checked per warp by the caller),
+// and every footprint is at least 1e-4 rows wide (also checked).
+template <int NT, bool LINEAR, bool CLAMP>
 __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int nu, int nv, int lbase,
-                                             const float *ov, float zfirst, float dzs, float hz, float Sz, float imin,
-                                             float imax, float Mv, float Av, float wscale, float *acc) {
+                                             const float *ov, float lo0, float hi0, float dlo, float dhi,
+                                             float zfirst, float dzs, float hz, float Sz, float imin, float imax,
+                                             float Mv, float Av, float wscale, float *acc) {
     const float fnv = (float)nv;
-    float lo0, hi0, dlo = 0.0f, dhi = 0.0f;
-    v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &lo0, &hi0);
-    if (LINEAR) {
-        float lo1, hi1;
-        v_footprint(zfirst + dzs, hz, Sz, imin, imax, Mv, Av, &lo1, &hi1);
-        dlo = lo1 - lo0;
-        dhi = hi1 - hi0;
-    }
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) {
         float vlo, vhi;
@@ -283,17 +279,37 @@ __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int 
         } else {
             v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &vlo, &vhi);
         }
-        const float width = vhi - vlo;
-        const float clo = fminf(fmaxf(vlo, 0.0f), fnv), chi = fminf(fmaxf(vhi, 0.0f), fnv);
+        const float rw = fast_rcp(vhi - vlo);
+        if (CLAMP) {
+            vlo = fminf(fmaxf(vlo, 0.0f), fnv);
+            vhi = fminf(fmaxf(vhi, 0.0f), fnv);
+        }
         float flo, fhi;
-        const int mlo = floor_split(clo, &flo), mhi = floor_split(chi, &fhi);
-        const float2 *rlo = IQ + (long long)mlo * nu + lbase;
-        const float2 *rhi = IQ + (long long)mhi * nu + lbase;
-        const float integ = integ_taps<NT>(rlo, rhi, clo - flo, chi - fhi, ov);
-        // A footprint narrower than a detector row lies in one row: weight 1.
-        const float val = (width > 1e-6f) ? integ * fast_rcp(width) : integ_taps<NT>(rlo, rlo, 0.0f, 1.0f, ov);
-        acc[j] = fmaf(val, wscale, acc[j]);
+        const int mlo = floor_split(vlo, &flo), mhi = floor_split(vhi, &fhi);
+        const float2 *rlo = IQ + mlo * nu + lbase;
+        const float2 *rhi = IQ + mhi * nu + lbase;
+        const float ulo = vlo - flo, uhi = vhi - fhi;
+        float s = 0.0f;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            const float2 a = __ldg(rlo + t), b = __ldg(rhi + t);
+            s = fmaf(ov[t], fmaf(b.y, uhi, b.x) - fmaf(a.y, ulo, a.x), s);
+        }
+        acc[j] = fmaf(s * rw, wscale, acc[j]);
     }
+}
+
+template <int NT, bool LINEAR>
+__device__ __forceinline__ void integ_dispatch(bool clamp, const float2 *__restrict__ IQ, int nu, int nv, int lbase,
+                                               const float *ov, float lo0, float hi0, float dlo, float dhi,
+                                               float zfirst, float dzs, float hz, float Sz, float imin, float imax,
+                                               float Mv, float Av, float wscale, float *acc) {
+    if (clamp)
+        integ_voxels<NT, LINEAR, true>(IQ, nu, nv, lbase, ov, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, imax,
+                                       Mv, Av, wscale, acc);
+    else
+        integ_voxels<NT, LINEAR, false>(IQ, nu, nv, lbase, ov, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin,
+                                        imax, Mv, Av, wscale, acc);
 }
 
 template <bool CURVED>
@@ -356,36 +372,60 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
         }
         if (uw > 1e-6f) wscale *= fast_rcp(uw);
         else { ov[0] = (l0 >= 0 && l0 < nu) ? 1.0f : 0.0f; ov[1] = ov[2] = ov[3] = 0.0f; }
-        // Clamp the tap base so every tap address lies inside the detector row.
-        const int lbase = min(max(l0, 0), max(nu - 4, 0));
-        // Weights re-aligned to the clamped base: tap t reads cell lbase + t,
-        // whose weight is ov[lbase + t - l0] (a select chain, not an indexed load).
-        const int shift = lbase - l0;
+        // Tap base inside the detector row; weights re-aligned only for the
+        // (rare) columns whose footprint touches a detector edge.
+        const bool inner = l0 >= 0 && l0 + 4 <= nu;
+        const int lbase = inner ? l0 : min(max(l0, 0), max(nu - 4, 0));
         float ovb[4];
+        if (__all_sync(0xffffffffu, inner)) {
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int src = t + shift;
-            float w = 0.0f;
+            for (int t = 0; t < 4; ++t) ovb[t] = ov[t];
+        } else {
+            const int shift = lbase - l0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) w = (src == k) ? ov[k] : w;
-            ovb[t] = w;
+            for (int t = 0; t < 4; ++t) {
+                const int src = t + shift;
+                float w = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) w = (src == k) ? ov[k] : w;
+                ovb[t] = w;
+            }
         }
         int ntl = 1;
 #pragma unroll
         for (int t = 1; t < 4; ++t) ntl = (ovb[t] > 0.0f) ? t + 1 : ntl;
-        const bool ok = live && imin > 0.0f && (uhi - fl0) <= 4.0f && nu >= 4;
-        const int nt = __reduce_max_sync(0xffffffffu, ok ? ntl : 1);
         const float Mv = (Dy - Sy) * inv_dv, Av = (Sz - pp0) * inv_dv;
         // Linear z regime: neither z end of any voxel in the chunk crosses S_z.
         const float ztop = fmaxf(zfirst, zend) + fabsf(hz), zbot = fminf(zfirst, zend) - fabsf(hz);
         const bool linear = (Sz - ztop > 0.0f) || (Sz - zbot < 0.0f);
+        float lo0, hi0, loN, hiN;
+        v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &lo0, &hi0);
+        v_footprint(zend, hz, Sz, imin, imax, Mv, Av, &loN, &hiN);
+        const float dlo = zlast > 0 ? (loN - lo0) / (float)zlast : 0.0f;
+        const float dhi = zlast > 0 ? (hiN - hi0) / (float)zlast : 0.0f;
+        const bool ok = live && imin > 0.0f && (uhi - fl0) <= 4.0f && nu >= 4 &&
+                        fminf(hi0 - lo0, hiN - loN) > 1e-4f;
+        const int nt = __reduce_max_sync(0xffffffffu, ok ? ntl : 1);
+        const float fnv = (float)nv;
+        const bool inside = fminf(fminf(lo0, loN), fminf(hi0, hiN)) >= 0.0f &&
+                            fmaxf(fmaxf(lo0, loN), fmaxf(hi0, hiN)) <= fnv;
+        // Clamped reads also for a partial last chunk, whose extrapolated
+        // voxels (beyond nz) must still address rows inside [0, nv].
+        const bool clamp = !__all_sync(0xffffffffu, inside || !ok) || zlast < kBiZ - 1;
         if (ok) {
             if (linear) {
-                if (nt <= 2) integ_voxels<2, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
-                else if (nt == 3) integ_voxels<3, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
-                else integ_voxels<4, true>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+                if (nt <= 2)
+                    integ_dispatch<2, true>(clamp, IQ, nu, nv, lbase, ovb, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz,
+                                            imin, imax, Mv, Av, wscale, acc);
+                else if (nt == 3)
+                    integ_dispatch<3, true>(clamp, IQ, nu, nv, lbase, ovb, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz,
+                                            imin, imax, Mv, Av, wscale, acc);
+                else
+                    integ_dispatch<4, true>(clamp, IQ, nu, nv, lbase, ovb, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz,
+                                            imin, imax, Mv, Av, wscale, acc);
             } else {
-                integ_voxels<4, false>(IQ, nu, nv, lbase, ovb, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, wscale, acc);
+                integ_voxels<4, false, true>(IQ, nu, nv, lbase, ovb, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin,
+                                             imax, Mv, Av, wscale, acc);
             }
         } else if (live) {
             // Reference weight calculators on the raw values (Q = the float2's y).
@@ -431,7 +471,7 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
 // ---- matched (adjoint) backprojector ---------------------------------------
 
 template <int A>
-__device__ float matched_voxel_view(const TableHeader &h, const float *__restrict__ T, const float *__restrict__ V,
+__device__ __noinline__ float matched_voxel_view(const TableHeader &h, const float *__restrict__ T, const float *__restrict__ V,
                                     const ViewOffsets &vo, const float *__restrict__ Q, int ix, int iy, int iz) {
     constexpr int B1 = Axes<A>::B1, B2 = Axes<A>::B2;
     const float d[3] = {h.dx, h.dy, h.dz};
@@ -621,6 +661,194 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
     }
 }
 
+// Matched backprojection over prescaled, integrated projections (default when
+// the caller supplies a workspace).  For x/y-dominant views the forward gives
+// pixel (r, c) the weight K_rc * g_s * ov_x(c; k, s) * ov_z(r; l, s) on voxel
+// (k, s, l) with ov_z the overlap, in voxel units, of row r's z interval on
+// slice s with [l, l+1].  The rows of column c tile that axis with a pitch of
+// |dB * tau_c| voxels, so sum_r y'_r ov_z = |dB tau_c| (C(r_hi) - C(r_lo)),
+// C the running sum of y' = y * K down the column and r_lo, r_hi the voxel's
+// boundaries in row coordinates.  matched_integrate_kernel writes (C, y') as
+// float2; z-dominant views read the raw projections instead.
+__global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
+                                         float2 *__restrict__ out, int view0, int nviews) {
+    const TableHeader &h = header(T);
+    const int nu = h.nu, nv = h.nv;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * nviews) return;
+    const int vi = (int)(t / nu), c = (int)(t % nu);
+    const ViewOffsets vo = view_offsets(nu, nv);
+    const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+    const int axis = (int)V[VF_AXIS];
+    const float *__restrict__ q = proj + (long long)vi * nu * nv + c;
+    float2 *__restrict__ o = out + (long long)vi * (nv + 1) * nu + c;
+    double run = 0.0;
+    if (axis == 2) {
+        for (int r = 0; r < nv; ++r) o[(long long)r * nu] = make_float2(0.0f, __ldg(q + (long long)r * nu));
+        o[(long long)nv * nu] = make_float2(0.0f, 0.0f);
+        return;
+    }
+    const bool xd = axis == 0;
+    const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
+    const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
+    const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
+    const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
+    const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
+    const float *__restrict__ Bzr = V + vo.bz;
+    const float *__restrict__ Pzr = V + vo.pz;
+    const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
+    const float inv_db = 1.0f / db, inv_dz = 1.0f / h.dz;
+    // The forward's per-pixel factor (dd_forward_tma_kernel epilogue), same expressions.
+    const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
+    const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
+    const float invD = 1.0f / (Sa - Pa[c]);
+    const float t1 = (Sb - Pb[c]) * invD;
+    const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
+    float Bprev = (Sz - Bzr[0]) * inv_dz;
+    for (int r = 0; r < nv; ++r) {
+        const float Bnext = (Sz - Bzr[r + 1]) * inv_dz;
+        const float t2 = (Sz - Pzr[r]) * invD;
+        const float K = base * sqrtf(1.0f + t2 * t2) / fabsf(Bnext - Bprev);
+        const float y = __ldg(q + (long long)r * nu) * K;
+        o[(long long)r * nu] = make_float2((float)run, y);
+        run += y;
+        Bprev = Bnext;
+    }
+    o[(long long)nv * nu] = make_float2((float)run, 0.0f);
+}
+
+constexpr int kMC = 6;   // detector columns kept per (voxel column, view); more -> per-voxel path
+
+__global__ void __launch_bounds__(kBpTileX * kBpTileY, 4)
+bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
+                        const float *__restrict__ proj, float *__restrict__ vol, int view0, int nviews, float scale,
+                        int accumulate) {
+    const TableHeader &h = header(T);
+    const int ix = blockIdx.x * kBpTileX + threadIdx.x;
+    const int iy = blockIdx.y * kBpTileY + threadIdx.y;
+    const int l0 = blockIdx.z * kMZ;
+    const bool live = ix < h.nx && iy < h.ny;
+    const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
+    const int nu = h.nu, nv = h.nv, nz = h.nz;
+    const ViewOffsets vo = view_offsets(nu, nv);
+    const float *__restrict__ pzp = T + h.off_zplane;
+    const float inv_dz = 1.0f / h.dz;
+    const float fnv = (float)nv;
+    float acc[kMZ];
+#pragma unroll
+    for (int j = 0; j < kMZ; ++j) acc[j] = 0.0f;
+
+    for (int vi = 0; vi < nviews; ++vi) {
+        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+        const float2 *__restrict__ IQ = integ + (long long)vi * (nv + 1) * nu;
+        const int axis = (int)V[VF_AXIS];
+        const float *__restrict__ Qraw = proj + (long long)vi * nu * nv;
+        if (axis == 2) {
+            // z-dominant: per-voxel candidate search on the raw values.
+            if (!live) continue;
+#pragma unroll
+            for (int j = 0; j < kMZ; ++j)
+                if (l0 + j < nz) acc[j] += matched_voxel_view<2>(h, T, V, vo, Qraw, ixc, iyc, l0 + j);
+            continue;
+        }
+        const bool xd = axis == 0;
+        const int s = xd ? ixc : iyc, k = xd ? iyc : ixc;
+        const float *__restrict__ pa = T + (xd ? h.off_xplane : h.off_yplane);
+        const float *__restrict__ pb = T + (xd ? h.off_yplane : h.off_xplane);
+        const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
+        const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
+        const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
+        const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
+        const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
+        const float *__restrict__ Bzr = V + vo.bz;
+        const float inv_db = 1.0f / db;
+        const float Cb = (Sb - pb[0]) * inv_db;
+        const float A = (Sz - pzp[0]) * inv_dz;
+        const float q = pa[s] + 0.5f * da - Sa;
+        const float g = 1.0f / (q * q);
+        const float B0 = (Sz - Bzr[0]) * inv_dz;
+        const float dB = ((Sz - Bzr[nv]) * inv_dz - B0) / fnv;       // row pitch of B
+        // Candidate columns: project the voxel's transverse edges on the slice centre plane.
+        float cmin = INFINITY, cmax = -INFINITY;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float bw = pb[k + e];
+            const float pcw = pa[s] + 0.5f * da;
+            const float ddx = (xd ? pcw : bw) - V[VF_SX];
+            const float ddy = (xd ? bw : pcw) - V[VF_SY];
+            const float aa = ddx * V[VF_EUX] + ddy * V[VF_EUY], bb = ddx * V[VF_EWX] + ddy * V[VF_EWY];
+            const float u = h.curved ? atan2f(aa, bb) : h.sdd * aa / bb;
+            const float cu = (u - h.u0_fwd) / h.du_fwd;
+            cmin = fminf(cmin, cu); cmax = fmaxf(cmax, cu);
+        }
+        const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
+        const float kf = (float)k;
+        // Up to kMC columns with ov_x > 0 (the same x' expressions as the forward).
+        int ncol = 0;
+        int cc[kMC];
+        float wcol[kMC], al[kMC], be[kMC];
+#pragma unroll
+        for (int m = 0; m < kMC; ++m) { cc[m] = 0; wcol[m] = 0.0f; al[m] = 0.0f; be[m] = 0.0f; }
+        bool overflow = false;
+        for (int c = cA; c <= cB; ++c) {
+            const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
+            const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
+            const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
+            const float ovx = fminf(kf + 1.0f, fmaxf(xa, xb)) - fmaxf(kf, fminf(xa, xb));
+            if (!(ovx > 0.0f)) continue;
+            const float tau = q * (1.0f / (Sa - Pa[c]));
+            // voxel boundary z' -> row coordinate: r = ((z' - A) / tau - B0) / dB
+            const float inv = 1.0f / (tau * dB);
+            const float wz = fabsf(dB * tau);
+            if (ncol < kMC) {
+#pragma unroll
+                for (int m = 0; m < kMC; ++m)
+                    if (m == ncol) { cc[m] = c; wcol[m] = ovx * g * wz; al[m] = (-A / tau - B0) / dB; be[m] = inv; }
+                ++ncol;
+            } else {
+                overflow = true;
+            }
+        }
+        if (overflow) {
+            // Detector columns much narrower than a voxel: per-voxel search.
+            if (!live) continue;
+#pragma unroll
+            for (int j = 0; j < kMZ; ++j) {
+                if (l0 + j >= nz) continue;
+                acc[j] += xd ? matched_voxel_view<0>(h, T, V, vo, Qraw, ixc, iyc, l0 + j)
+                             : matched_voxel_view<1>(h, T, V, vo, Qraw, ixc, iyc, l0 + j);
+            }
+            continue;
+        }
+        if (!live) continue;
+#pragma unroll
+        for (int m = 0; m < kMC; ++m) {
+            if (m >= ncol) break;
+            const float2 *__restrict__ colp = IQ + cc[m];
+#pragma unroll
+            for (int j = 0; j < kMZ; ++j) {
+                const float ra = fmaf((float)(l0 + j), be[m], al[m]);
+                const float rb = ra + be[m];
+                const float lo = fminf(fmaxf(fminf(ra, rb), 0.0f), fnv), hi = fminf(fmaxf(fmaxf(ra, rb), 0.0f), fnv);
+                float flo, fhi;
+                const int mlo = floor_split(lo, &flo), mhi = floor_split(hi, &fhi);
+                const float2 a = __ldg(colp + (long long)mlo * nu), b = __ldg(colp + (long long)mhi * nu);
+                const float integ_v = fmaf(b.y, hi - fhi, b.x) - fmaf(a.y, lo - flo, a.x);
+                acc[j] = fmaf(integ_v, wcol[m], acc[j]);
+            }
+        }
+    }
+    if (!live) return;
+#pragma unroll
+    for (int j = 0; j < kMZ; ++j) {
+        const int iz = l0 + j;
+        if (iz < nz) {
+            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
+            *dst = accumulate ? *dst + scale * acc[j] : scale * acc[j];
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kBpTileX * kBpTileY)
 bp_matched_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
                   int nviews, float scale, int accumulate) {
@@ -739,5 +967,41 @@ extern "C" int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_integ_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_table, const float *d_proj,
+                                           float *d_vol, int32_t view0, int32_t nviews, float scale,
+                                           int32_t accumulate, void *d_workspace, size_t workspace_bytes,
+                                           void *stream) {
+    clear_error();
+    int st = bp_args(p, d_table, d_proj, d_vol, view0, nviews, "ctgb_backproject_matched_ws");
+    if (st) return st;
+    if (!d_workspace) return set_error(CTGB_ERR_ARG, "ctgb_backproject_matched_ws: NULL workspace");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nviews == 0) {
+        if (!accumulate) {
+            cudaError_t e = cudaMemsetAsync(d_vol, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nz, s);
+            if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
+        return CTGB_OK;
+    }
+    const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    const int chunk = (int)(workspace_bytes / per_view);
+    if (chunk < 1) return set_error(CTGB_ERR_SIZE, "ctgb_backproject_matched_ws: workspace below one view");
+    const float *T = static_cast<const float *>(d_table);
+    float2 *ws = static_cast<float2 *>(d_workspace);
+    dim3 block(kBpTileX, kBpTileY);
+    dim3 grid((p->nx + kBpTileX - 1) / kBpTileX, (p->ny + kBpTileY - 1) / kBpTileY, (p->nz + kMZ - 1) / kMZ);
+    for (int v = 0; v < nviews; v += chunk) {
+        const int n = nviews - v < chunk ? nviews - v : chunk;
+        const long long threads = (long long)p->nu * n;
+        const float *pv = d_proj + (long long)v * p->nu * p->nv;
+        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, pv, ws, view0 + v, n);
+        const int acc = (v > 0) ? 1 : accumulate;
+        bp_matched_integ_kernel<<<grid, block, 0, s>>>(T, ws, pv, d_vol, view0 + v, n, scale, acc);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_integ_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
 }

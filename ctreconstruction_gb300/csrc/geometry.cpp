@@ -231,6 +231,12 @@ static FilterHeader filter_layout(const ctgb_params *p) {
 //              python/FanBeam.py:175-209) — spectrum doubled, cutoff |w| > pi*cutoff
 //   variant 2: equiangular kernel of matlab/FilterArc.m (odd taps
 //              -1/(2 pi^2 tau^2 sin^2(n tau))), cutoff as variant 0
+//   variant 3: equiangular kernel of Kak & Slaney, "Principles of
+//              Computerized Tomographic Imaging" eq. (3.124) (odd taps
+//              -1/(2 pi^2 sin^2(n tau)), centre 1/(8 tau^2)), cutoff
+//              |w| > pi*cutoff.  FilterArc.m keeps an extra tau^2 in the odd
+//              taps, which unbalances the kernel for small channel angles;
+//              this variant is the one that reconstructs quantitatively.
 static std::vector<double> ramp_spectrum(int N, double tau, int type, double cutoff, int variant = 0) {
     const int M = N - 1;
     std::vector<double> h(M), x(N);
@@ -241,9 +247,9 @@ static std::vector<double> ramp_spectrum(int N, double tau, int type, double cut
         if (m < 0) m += 2.0;   // numpy's % follows the divisor's sign
         if (xi == 0) h[i] = 1.0 / (8.0 * tau * tau);
         else if (m == 1.0) {
-            if (variant == 2) {
+            if (variant == 2 || variant == 3) {
                 const double sn = std::sin(xi * tau);
-                h[i] = -1.0 / (2.0 * M_PI * M_PI * tau * tau * sn * sn);
+                h[i] = -1.0 / (2.0 * M_PI * M_PI * (variant == 2 ? tau * tau : 1.0) * sn * sn);
             } else {
                 h[i] = -0.5 / ((M_PI * tau * xi) * (M_PI * tau * xi));
             }
@@ -276,7 +282,7 @@ static std::vector<double> ramp_spectrum(int N, double tau, int type, double cut
             case 4: f *= (0.5 + 0.5 * std::cos(w / cutoff)); break;
             default: break;
         }
-        const double lim = (variant == 1) ? M_PI * cutoff : M_PI * cutoff / (2.0 * tau);
+        const double lim = (variant == 1 || variant == 3) ? M_PI * cutoff : M_PI * cutoff / (2.0 * tau);
         if (std::fabs(w) > lim) f = 0;
         filt[k] = f;
     }
@@ -354,7 +360,8 @@ extern "C" int ctgb_standalone_filter_bytes(const ctgb_conebeam_params *p, size_
 //   at iso-scaled pixel centres, rows flipped along u, no deltaS;
 // variant 1 fan line (FanBeam.py:111-122): weight R/sqrt(R^2+gamma^2), no deltaS;
 // variant 2 fan arc (matlab/FanBeamReconArc.m:13-27): weight D*dgamma*cos(gamma),
-//   arc kernel, gamma = channel angle (pitch pixel_width / SDD).
+//   arc kernel, gamma = channel angle (pitch pixel_width / SDD);
+// variant 3 fan arc with the balanced equiangular kernel (same weight).
 extern "C" int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32_t variant, int32_t filter_type,
                                             double cutoff, void *host_buf, size_t bytes) {
     size_t need = 0;
@@ -362,7 +369,7 @@ extern "C" int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32
     if (st) return st;
     if (!host_buf || bytes < need) return set_error(CTGB_ERR_SIZE, "filter buffer too small");
     if (filter_type < 0 || filter_type > 4) return set_error(CTGB_ERR_ARG, "unknown filter type");
-    if (variant < 0 || variant > 2) return set_error(CTGB_ERR_ARG, "unknown filter variant");
+    if (variant < 0 || variant > 3) return set_error(CTGB_ERR_ARG, "unknown filter variant");
     if (!(cutoff > 0)) return set_error(CTGB_ERR_ARG, "cutoff must be positive");
     std::memset(host_buf, 0, need);
     FilterHeader f = sa_layout(p);
@@ -371,9 +378,9 @@ extern "C" int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32
     const int nu = p->det_width, nv = p->det_height;
     std::vector<double> filt;
     double scale = 1.0;
-    if (variant == 2) {
+    if (variant >= 2) {
         const double dg = p->pixel_width / p->source_to_detector;   // channel angle
-        filt = ramp_spectrum(f.zpl + 1, dg, filter_type, cutoff, 2);
+        filt = ramp_spectrum(f.zpl + 1, dg, filter_type, cutoff, variant);
         scale = R * dg;
         f.R = (float)R;
         for (int j = 0; j < nu; ++j) B[f.off_kk + j] = (float)(R * std::tan((j - (nu - 1) / 2.0) * dg));

@@ -94,7 +94,14 @@ AUTOTUNER = TileAutotuner()
 
 
 class FanBatch:
-    def __init__(self, slices, device=None, filter_type='hann', cutoff=0.3, autotuner=AUTOTUNER, tile=None):
+    def __init__(self, slices, device=None, filter_type='hann', cutoff=0.3, autotuner=AUTOTUNER, tile=None,
+                 arc_kernel='reference'):
+        """arc_kernel: 'reference' filters arc-detector slices with
+        matlab/FilterArc.m's kernel; 'balanced' with the Kak & Slaney
+        equiangular kernel (quantitative reconstructions)."""
+        if arc_kernel not in ('reference', 'balanced'):
+            raise ValueError("arc_kernel must be 'reference' or 'balanced'")
+        self.arc_kernel = arc_kernel
         self.slices = list(slices)
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.filter_type = filter_type
@@ -130,7 +137,8 @@ class FanBatch:
             n = ctypes.c_size_t(0)
             _lib.call("ctgb_standalone_filter_bytes", ctypes.byref(c), ctypes.byref(n))
             host = np.zeros(n.value // 4, dtype=np.float32)
-            _lib.call("ctgb_standalone_filter_build", ctypes.byref(c), 2 if s.arc else 1,
+            variant = (3 if self.arc_kernel == 'balanced' else 2) if s.arc else 1
+            _lib.call("ctgb_standalone_filter_build", ctypes.byref(c), variant,
                       _lib.FILTER_TYPES[self.filter_type], float(self.cutoff), host.ctypes.data_as(ctypes.c_void_p),
                       n.value)
             zpl = ctypes.c_int32(0)

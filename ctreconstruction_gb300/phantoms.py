@@ -81,3 +81,63 @@ def random_ellipsoids(shape, n=30, seed=1, axes=(0.05, 0.3), values=(-0.2, 0.5),
         val = rng.uniform(values[0], values[1])
         _add_ellipsoid(vol, z, y, x, float(val), tuple(ax), tuple(centre), _random_rotation(rng))
     return vol
+
+
+def random_ellipses(count=20, seed=0, axes=(0.03, 0.3), values=(-0.1, 0.4), radius=0.8):
+    """`count` ellipses (value, cx, cy, a, b, phi) in units of the image
+    half-width: centres uniform in the disk of the given radius, semi-axes
+    U(axes), angles U(0, pi), additive values U(values)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        r = radius * math.sqrt(rng.random())
+        t = 2 * math.pi * rng.random()
+        a, b = rng.uniform(axes[0], axes[1], 2)
+        out.append((float(rng.uniform(values[0], values[1])), r * math.cos(t), r * math.sin(t), float(a), float(b),
+                    float(rng.uniform(0, math.pi))))
+    return out
+
+
+def ellipse_image(ellipses, x, y):
+    """Image [len(y)][len(x)] of the ellipses sampled at the pixel centres
+    x (ascending) and y; ellipse coordinates are physical (same units)."""
+    Y, X = torch.meshgrid(y, x, indexing="ij")
+    img = torch.zeros(Y.shape, dtype=torch.float32, device=Y.device)
+    for val, cx, cy, a, b, phi in ellipses:
+        xr = (X - cx) * math.cos(phi) + (Y - cy) * math.sin(phi)
+        yr = -(X - cx) * math.sin(phi) + (Y - cy) * math.cos(phi)
+        img += val * (((xr / a) ** 2 + (yr / b) ** 2) <= 1.0).float()
+    return img
+
+
+def ellipse_fan_sinogram(ellipses, R, nviews, gammas, dtheta, arc=False, theta0=0.0, device="cuda"):
+    """Exact line integrals of the ellipses along fan rays, [nviews][nch].
+
+    View i has its source at angle theta = theta0 + i*dtheta on the circle of
+    radius R: in the rotated frame t = x cos + y sin, s = -x sin + y cos the
+    source sits at (t, s) = (0, R).  Channel j's ray passes through the
+    point (t, s) = (u_j, 0) with u_j = gammas[j] (line detector, channel
+    positions scaled to the axis) or u_j = R tan(gammas[j]) (arc detector,
+    channel angles) — the geometry the fan backprojector inverts."""
+    th = theta0 + dtheta * torch.arange(nviews, dtype=torch.float64, device=device)
+    g = torch.as_tensor(gammas, dtype=torch.float64, device=device)
+    u = R * torch.tan(g) if arc else g
+    c, s = torch.cos(th)[:, None], torch.sin(th)[:, None]
+    sx, sy = -R * s, R * c                                  # source (x, y)
+    px, py = u[None] * c, u[None] * s                       # point on the central line
+    dx, dy = px - sx, py - sy
+    nrm = torch.sqrt(dx * dx + dy * dy)
+    dx, dy = dx / nrm, dy / nrm
+    sino = torch.zeros((nviews, g.numel()), dtype=torch.float64, device=device)
+    for val, cx, cy, a, b, phi in ellipses:
+        cp, sp = math.cos(phi), math.sin(phi)
+        ox, oy = sx - cx, sy - cy
+        p1 = (ox * cp + oy * sp) / a
+        p2 = (-ox * sp + oy * cp) / b
+        d1 = (dx * cp + dy * sp) / a
+        d2 = (-dx * sp + dy * cp) / b
+        dd = d1 * d1 + d2 * d2
+        pd = p1 * d1 + p2 * d2
+        disc = pd * pd - dd * (p1 * p1 + p2 * p2 - 1.0)
+        sino += val * 2.0 * torch.sqrt(torch.clamp(disc, min=0.0)) / dd
+    return sino.float()

@@ -128,8 +128,13 @@ class Projector:
             out = torch.empty(self.volume_shape, dtype=torch.float32, device=proj.device)
             accumulate = False
         self._check(out, self.volume_shape, "out")
-        _lib.call("ctgb_backproject_matched", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out), view0,
-                  nviews, float(scale), int(bool(accumulate)), _stream())
+        ws = self._workspace(nviews)
+        if ws is None:
+            _lib.call("ctgb_backproject_matched", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out),
+                      view0, nviews, float(scale), int(bool(accumulate)), _stream())
+        else:
+            _lib.call("ctgb_backproject_matched_ws", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out),
+                      view0, nviews, float(scale), int(bool(accumulate)), _ptr(ws), ws.numel() * 4, _stream())
         return out
 
     # -- FDK filtering --------------------------------------------------------

@@ -113,6 +113,12 @@ int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table, const flo
  * vol = (accumulate ? vol : 0) + scale * A^T proj. */
 int ctgb_backproject_matched(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                              int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
+/* Same result, faster: projections prescaled by the forward's per-pixel
+ * factor and integrated along v into a caller-supplied workspace (size as for
+ * ctgb_backproject_fdk_workspace_bytes), processed in view chunks that fit. */
+int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                                int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
+                                size_t workspace_bytes, void *stream);
 
 /* ---- FDK filtering ----------------------------------------------------------
  * Replaces Reconstruction.Filtering()/filter_proj/Filter
@@ -155,8 +161,10 @@ int ctgb_conebeam_backproject(const ctgb_conebeam_params *p, const void *d_table
 /* Filter tables of the standalone reconstructors (ConeBeam.Filter / FanBeam.Filter,
  * python/ConeBeamGPU.py:353-379, python/FanBeam.py:175-209; arc kernel
  * matlab/FilterArc.m): variant 0 cone beam (cosine weight over u and v, rows
- * flipped along u as ConeBeamGPU.py:298 does), 1 fan line, 2 fan arc.  Same
- * layout as ctgb_filter_build; apply with ctgb_filter_apply. */
+ * flipped along u as ConeBeamGPU.py:298 does), 1 fan line, 2 fan arc, 3 fan
+ * arc with the balanced equiangular kernel (odd taps -1/(2 pi^2 sin^2(n tau)),
+ * cutoff |w| > pi*cutoff; FilterArc.m's kernel keeps an extra tau^2 there).
+ * Same layout as ctgb_filter_build; apply with ctgb_filter_apply. */
 int ctgb_standalone_filter_bytes(const ctgb_conebeam_params *p, size_t *bytes);
 int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32_t variant, int32_t filter_type, double cutoff,
                                  void *host_buf, size_t bytes);

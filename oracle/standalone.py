@@ -14,16 +14,18 @@ import numpy as np
 FILTERS = ('ram-lak', 'shepp-logan', 'cosine', 'hamming', 'hann')
 
 
-def standalone_filter(N, tau, filter_type, cutoff, arc=False):
+def standalone_filter(N, tau, filter_type, cutoff, arc=False, balanced=False):
     """ConeBeam.Filter / FanBeam.Filter (ConeBeamGPU.py:353-379, FanBeam.py:175-209):
     spectrum doubled, cutoff |w| > pi*cutoff.  arc: matlab/FilterArc.m kernel
-    (odd taps -1/(2 pi^2 tau^2 sin^2(n tau))), not doubled, cutoff |w| > pi*cutoff/(2 tau)."""
+    (odd taps -1/(2 pi^2 tau^2 sin^2(n tau))), not doubled, cutoff |w| > pi*cutoff/(2 tau).
+    arc and balanced: Kak & Slaney eq. (3.124) kernel (odd taps
+    -1/(2 pi^2 sin^2(n tau))), not doubled, cutoff |w| > pi*cutoff."""
     x = np.arange(0, N) - (N - 1) / 2
     h = np.zeros(len(x))
     h[x == 0] = 1 / (8 * tau ** 2)
     odd = np.mod(x, 2) == 1
     if arc:
-        h[odd] = -1.0 / (2 * np.pi ** 2 * tau ** 2 * np.sin(x[odd] * tau) ** 2)
+        h[odd] = -1.0 / (2 * np.pi ** 2 * (1.0 if balanced else tau ** 2) * np.sin(x[odd] * tau) ** 2)
     else:
         h[odd] = -0.5 / (np.pi * tau * x[odd]) ** 2
     h = h[:-1]
@@ -41,7 +43,7 @@ def standalone_filter(N, tau, filter_type, cutoff, arc=False):
             filt = filt * (0.54 + 0.46 * np.cos(w / cutoff))
         elif filter_type == 'hann':
             filt = filt * (0.5 + 0.5 * np.cos(w / cutoff))
-    lim = np.pi * cutoff / (2 * tau) if arc else np.pi * cutoff
+    lim = np.pi * cutoff / (2 * tau) if (arc and not balanced) else np.pi * cutoff
     filt[np.abs(w) > lim] = 0
     return filt
 
@@ -119,14 +121,14 @@ def conebeam_backproject(p, Q):
     return recon
 
 
-def fan_filter(sino, R, sdd, pw, arc=False, filter_type='hann', cutoff=0.3):
+def fan_filter(sino, R, sdd, pw, arc=False, filter_type='hann', cutoff=0.3, balanced=False):
     """One slice's sinogram [ns][nch] -> Q (FanBeam.py:106-122 / FanBeamReconArc.m:20-27)."""
     nch = sino.shape[-1]
     zpl = _zpl(nch)
     if arc:
         dg = pw / sdd
         gam = (np.arange(nch) - (nch - 1) / 2) * dg
-        filt = standalone_filter(zpl + 1, dg, filter_type, cutoff, arc=True)
+        filt = standalone_filter(zpl + 1, dg, filter_type, cutoff, arc=True, balanced=balanced)
         wp = np.asarray(sino, np.float64) * (R * dg * np.cos(gam))[None]
     else:
         tau = pw * R / sdd
