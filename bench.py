@@ -217,11 +217,17 @@ def run_ours(args):
     bp = torch.empty(P.volume_shape, dtype=torch.float32, device=dev)
     xzy = torch.empty((n, n, n), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
-    ev = {k: [] for k in ("transpose", "forward", "backproject_fdk")}
+    integ = P.integrate(proj)                          # integrated-projection workspace (float2 per cell)
+    names = ("transpose", "forward", "integrate", "backproject_fdk")
+    ev = {k: [] for k in names}
+    # backward() = integrate (integrate_rows_kernel) + bp_fdk_integ_kernel:
+    # the same two launches ctgb_backproject_fdk_ws makes, issued one by one
+    # so that each kernel is timed alone.
+    launches_per_step = 1 + P.forward_launches() + 2
 
     def step(record=False):
         if record:
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
             e[0].record(stream)
         P.transpose(vol, out=xzy)
         if record:
@@ -229,12 +235,14 @@ def run_ours(args):
         P.forward(vol, out=proj, transposed=xzy)
         if record:
             e[2].record(stream)
-        P.backproject_fdk(proj, out=bp)
+        P.integrate(proj, out=integ)
         if record:
             e[3].record(stream)
-            ev["transpose"].append((e[0], e[1]))
-            ev["forward"].append((e[1], e[2]))
-            ev["backproject_fdk"].append((e[2], e[3]))
+        P.backproject_fdk_integrated(integ, out=bp)
+        if record:
+            e[4].record(stream)
+            for k, name in enumerate(names):
+                ev[name].append((e[k], e[k + 1]))
 
     def barrier():
         if ws > 1:
@@ -260,14 +268,20 @@ def run_ours(args):
     value = ws * vv / (ms / 1e3) / 1e9
 
     kern = {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in ev.items()}
+    # Dominant kernel: bp_fdk_integ_kernel (one launch over all views) or the
+    # forward (dd_forward_tma_kernel, one launch per run of same-axis views).
+    nfwd = P.forward_launches()
+    per_launch = {"forward": kern["forward"] / nfwd, "backproject_fdk": kern["backproject_fdk"]}
     dom = max(("forward", "backproject_fdk"), key=lambda k: kern[k])
     peak, peak_kind = measured_peaks()
-    alg_bytes = 4.0 * vv                 # 4 B per voxel-view per direction
-    achieved = alg_bytes / (kern[dom] / 1e3) / 1e9
-    kname = {"forward": "dd_forward_kernel", "backproject_fdk": "bp_fdk_kernel"}[dom]
+    units = {"forward": vv / nfwd, "backproject_fdk": vv}[dom]      # voxel-views per launch
+    alg_bytes = 4.0 * units              # 4 B per voxel-view per direction
+    achieved = alg_bytes / (per_launch[dom] / 1e3) / 1e9
+    kname = {"forward": "dd_forward_tma_kernel", "backproject_fdk": "bp_fdk_integ_kernel"}[dom]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(kname),
-                "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": kern[dom]}
+                "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": per_launch[dom],
+                "per_kernel_frac": {k: 4.0 * vv / (kern[k] / 1e3) / 1e9 / peak for k in ("forward", "backproject_fdk")}}
 
     # matched pair (autograd path): forward + exact adjoint
     matched = None
@@ -321,7 +335,7 @@ def run_ours(args):
                            "step": "forward() + backward() (DD forward, FDK-weighted DD backprojection)",
                            "l2": "inputs larger than L2 (volume 512 MiB, projections 2.16 GiB)",
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
-                "kernels_ms": kern, "gpu_launches": 3 * args.steps, "effective_hbm_gbs": 2 * 4 * vv / (ms / 1e3) / 1e9,
+                "kernels_ms": kern, "gpu_launches": launches_per_step * args.steps, "effective_hbm_gbs": 2 * 4 * vv / (ms / 1e3) / 1e9,
                 "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "matched_pair": matched}
         print(json.dumps(line))
     if ws > 1:
@@ -443,14 +457,17 @@ def run_fan_batch(args):
 
 
 def run_iter(args):
-    """Batched OS-SART (10 subsets x 20 iterations, lambda 0.8) and MLEM (50
-    iterations) over 16 cone-beam scans, volumes 128^3..384^3 (multiples of
-    16), 90 views, detector 2N x 2N at 1.5x the voxel pitch, random ellipsoids
-    with Poisson noise at I0 = 5e4.  Times one OS-SART iteration (all scans,
-    all subsets) and one MLEM iteration (all scans)."""
+    """Batched OS-SART (10 subsets, lambda 0.8) and MLEM over 16 cone-beam
+    scans, volumes 128^3..384^3 (multiples of 16), 90 views, detector 2N x 2N
+    at 1.5x the voxel pitch, random ellipsoids with Poisson noise at I0 =
+    5e4.  Each method's 16 scans advance together: one CUDA graph holds one
+    iteration of all of them (OS-SART: 10 subsets each), so an iteration is
+    one graph launch.  Reports ms per batch iteration and the implied time
+    of the configured runs (20 OS-SART iterations, 50 MLEM iterations)."""
     import torch
     from ctreconstruction_gb300 import Projector, iterative, phantoms
     sides = [int(round(v / 16.0)) * 16 for v in np.linspace(128, 384, 16)]
+    dev = torch.device("cuda", torch.cuda.current_device())
     scans = []
     for i, n in enumerate(sides):
         vox = 256.0 / n
@@ -458,37 +475,43 @@ def run_iter(args):
              'EndAngle': 2 * np.pi, 'NumberOfDetectorPixels': [2 * n, 2 * n],
              'DetectorPixelSize': [1.5 * vox, 1.5 * vox], 'NumberOfViews': 90,
              'ImagePixelSpacing': [vox, vox, vox], 'NumberOfImage': [n, n, n]}
-        P = Projector(p)
-        ph = phantoms.random_ellipsoids((n, n, n), n=30, seed=10 + i, device=P.device) * 0.01
+        P = Projector(p, device=dev)
+        ph = phantoms.random_ellipsoids((n, n, n), n=30, seed=10 + i, device=dev) * 0.01
         clean = P.forward(ph)
-        gen = torch.Generator(device=P.device).manual_seed(i)
+        gen = torch.Generator(device=dev).manual_seed(i)
         counts = torch.poisson(5e4 * torch.exp(-clean), generator=gen)
-        scans.append((P, -torch.log(torch.clamp(counts, min=1.0) / 5e4), ph))
-    t_os = t_em = 0.0
-    vv = 0
-    for P, proj, ph in scans:
-        x0 = torch.zeros(P.volume_shape, device=P.device)
-        iterative.os_sart(P, proj, nsubsets=10, niter=1, x0=x0)          # warm (workspaces, tables)
+        scans.append((p, -torch.log(torch.clamp(counts, min=1.0) / 5e4), ph))
+    vv = sum(float(n) ** 3 * 90 for n in sides)
+
+    def time_batch(batch, iters):
+        batch.capture()
+        batch.run(max(1, args.warmup))
+        torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        iterative.os_sart(P, proj, nsubsets=10, niter=2, x0=x0)
+        batch.run(iters)
         b.record()
         torch.cuda.synchronize()
-        t_os += a.elapsed_time(b) / 2
-        pc = proj.clone().clamp_(min=0)
-        iterative.mlem(P, pc, niter=1)
-        a.record()
-        iterative.mlem(P, pc, niter=2)
-        b.record()
-        torch.cuda.synchronize()
-        t_em += a.elapsed_time(b) / 2
-        vv += 2 * P.volume_shape[0] ** 3 * 90
-    return {"metric": "batched OS-SART / MLEM iteration throughput", "value": vv / ((t_os + t_em) / 2 / 1e3) / 1e9,
-            "unit": UNIT, "ms_per_step": (t_os + t_em) / 2, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic (random ellipsoids, Poisson I0=5e4)",
-            "config": {"workload": "os_sart_mlem_16scans_128to384_90views", "sides": sides},
+        return a.elapsed_time(b) / iters
+
+    os_batch = iterative.SolverBatch([iterative.OSSART(Projector(p, device=dev), q, nsubsets=10, lam=0.8)
+                                      for p, q, _ in scans])
+    t_os = time_batch(os_batch, max(1, args.steps))
+    os_rmse = [float(torch.sqrt(torch.mean((s.x - ph) ** 2))) for s, (_, _, ph) in zip(os_batch.solvers, scans)]
+    del os_batch
+    em_batch = iterative.SolverBatch([iterative.MLEM(Projector(p, device=dev), q.clamp(min=0)) for p, q, _ in scans])
+    t_em = time_batch(em_batch, max(1, args.steps))
+    del em_batch
+    # voxel-views per batch iteration: one forward + one backprojection per view
+    return {"metric": "batched OS-SART iteration throughput", "value": 2 * vv / (t_os / 1e3) / 1e9,
+            "unit": UNIT + " (forward + backprojection)", "ms_per_step": t_os, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (random ellipsoids, Poisson I0=5e4)",
+            "config": {"workload": "os_sart_mlem_16scans_128to384_90views", "sides": sides,
+                       "graph": "one CUDA graph launch per batch iteration"},
             "os_sart_ms_per_iteration": t_os, "mlem_ms_per_iteration": t_em,
-            "os_sart_20_iterations_s": 20 * t_os / 1e3, "mlem_50_iterations_s": 50 * t_em / 1e3}
+            "mlem_value": 2 * vv / (t_em / 1e3) / 1e9,
+            "os_sart_20_iterations_s": 20 * t_os / 1e3, "mlem_50_iterations_s": 50 * t_em / 1e3,
+            "os_sart_rmse_after_%d_iterations" % (2 + max(1, args.warmup) + max(1, args.steps)): os_rmse[:4]}
 
 
 def run_asd256(args):

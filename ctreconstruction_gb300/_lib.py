@@ -59,6 +59,9 @@ SIGNATURES = {
     "ctgb_backproject_fdk_workspace_bytes": [_P, _i32, ctypes.POINTER(_sz)],
     "ctgb_backproject_fdk_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],
     "ctgb_backproject_matched_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],
+    "ctgb_integrate_projections": [_P, _vp, _i32, _vp, _sz, _vp],
+    "ctgb_forward_launches": [_P, _i32, _i32, ctypes.POINTER(_i32)],
+    "ctgb_backproject_fdk_integrated": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_filter_bytes": [_P, ctypes.POINTER(_sz)],
     "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],
     "ctgb_fdk_filter": [_P, _vp, _vp, _i32, _vp],

@@ -30,6 +30,7 @@
 #include "dd_common.cuh"
 #include "status.h"
 #include "tma.cuh"
+#include "f32x2.cuh"
 
 namespace ctgb {
 
@@ -232,6 +233,10 @@ bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj,
 // FMA each.  Running sums are accumulated in double and stored rounded, so
 // each lookup carries one float32 rounding of the prefix, not a drifting sum.
 constexpr int kBiZ = 16;
+#ifndef CTGB_BI_BLOCKS
+#define CTGB_BI_BLOCKS 5
+#endif
+constexpr int kBiBlocks = CTGB_BI_BLOCKS;   // resident CTAs per SM the register budget is sized for
 
 __global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__restrict__ out, int nu, int nv,
                                       int nviews) {
@@ -264,12 +269,21 @@ __device__ __forceinline__ float integ_taps(const float2 *__restrict__ rlo, cons
 // CLAMP: some footprint of the chunk may leave the detector's rows [0, nv];
 // without it every footprint lies inside (checked per warp by the caller),
 // and every footprint is at least 1e-4 rows wide (also checked).
+//
+// The (lo, hi) ends of a voxel's footprint travel as one f32x2 pair through
+// the floor/fraction split, and each tap's (C, Q) float2 is accumulated as a
+// pair: SL = sum_t ov_t (C, Q)(lo row), SH likewise at the hi row, so the
+// footprint integral is (SH.C + uhi SH.Q) - (SL.C + ulo SL.Q).
 template <int NT, bool LINEAR, bool CLAMP>
 __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int nu, int nv, int lbase,
                                              const float *ov, float lo0, float hi0, float dlo, float dhi,
                                              float zfirst, float dzs, float hz, float Sz, float imin, float imax,
                                              float Mv, float Av, float wscale, float *acc) {
     const float fnv = (float)nv;
+    const f2x magic = f2_pack(12582912.0f, 12582912.0f);
+    f2x ovp[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) ovp[t] = f2_pack(ov[t], ov[t]);
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) {
         float vlo, vhi;
@@ -284,17 +298,25 @@ __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int 
             vlo = fminf(fmaxf(vlo, 0.0f), fnv);
             vhi = fminf(fmaxf(vhi, 0.0f), fnv);
         }
-        float flo, fhi;
-        const int mlo = floor_split(vlo, &flo), mhi = floor_split(vhi, &fhi);
+        const f2x vp = f2_pack(vlo, vhi);
+        const f2x tp = f2_add_rd(vp, magic);            // floor_split on both ends
+        const f2x up = f2_sub(vp, f2_sub(tp, magic));   // (ulo, uhi) fractions
+        float tlo, thi, ulo, uhi;
+        f2_unpack(tp, tlo, thi);
+        f2_unpack(up, ulo, uhi);
+        const int mlo = __float_as_int(tlo) - 0x4B400000, mhi = __float_as_int(thi) - 0x4B400000;
         const float2 *rlo = IQ + mlo * nu + lbase;
         const float2 *rhi = IQ + mhi * nu + lbase;
-        const float ulo = vlo - flo, uhi = vhi - fhi;
-        float s = 0.0f;
+        f2x sl = f2_mul(ovp[0], f2_ldg(rlo)), sh = f2_mul(ovp[0], f2_ldg(rhi));
 #pragma unroll
-        for (int t = 0; t < NT; ++t) {
-            const float2 a = __ldg(rlo + t), b = __ldg(rhi + t);
-            s = fmaf(ov[t], fmaf(b.y, uhi, b.x) - fmaf(a.y, ulo, a.x), s);
+        for (int t = 1; t < NT; ++t) {
+            sl = f2_fma(ovp[t], f2_ldg(rlo + t), sl);
+            sh = f2_fma(ovp[t], f2_ldg(rhi + t), sh);
         }
+        float slc, slq, shc, shq;
+        f2_unpack(sl, slc, slq);
+        f2_unpack(sh, shc, shq);
+        const float s = fmaf(uhi, shq, shc) - fmaf(ulo, slq, slc);
         acc[j] = fmaf(s * rw, wscale, acc[j]);
     }
 }
@@ -313,7 +335,7 @@ __device__ __forceinline__ void integ_dispatch(bool clamp, const float2 *__restr
 }
 
 template <bool CURVED>
-__global__ void __launch_bounds__(kBpTX * kBpTY, 6)
+__global__ void __launch_bounds__(kBpTX * kBpTY, kBiBlocks)
 bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ, float *__restrict__ vol,
                     int view0, int nviews, float scale, int accumulate) {
     const TableHeader &h = header(T);
@@ -334,6 +356,7 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
     const float zfirst = T[h.off_zpix + min(z0, nz - 1)];
     const int zlast = min(z0 + kBiZ, nz) - 1 - z0;
     const float zend = zfirst + (float)zlast * dzs;
+    const float inv_zlast = zlast > 0 ? 1.0f / (float)zlast : 0.0f;
     float acc[kBiZ];
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) acc[j] = 0.0f;
@@ -401,8 +424,7 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
         float lo0, hi0, loN, hiN;
         v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &lo0, &hi0);
         v_footprint(zend, hz, Sz, imin, imax, Mv, Av, &loN, &hiN);
-        const float dlo = zlast > 0 ? (loN - lo0) / (float)zlast : 0.0f;
-        const float dhi = zlast > 0 ? (hiN - hi0) / (float)zlast : 0.0f;
+        const float dlo = (loN - lo0) * inv_zlast, dhi = (hiN - hi0) * inv_zlast;
         const bool ok = live && imin > 0.0f && (uhi - fl0) <= 4.0f && nu >= 4 &&
                         fminf(hi0 - lo0, hiN - loN) > 1e-4f;
         const int nt = __reduce_max_sync(0xffffffffu, ok ? ntl : 1);
@@ -965,6 +987,52 @@ extern "C" int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table
         else
             bp_fdk_integ_kernel<false><<<grid, block, 0, s>>>(T, ws, d_vol, view0 + v, n, scale, acc);
     }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_integ_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_integrate_projections(const ctgb_params *p, const float *d_proj, int32_t nviews,
+                                          void *d_workspace, size_t workspace_bytes, void *stream) {
+    clear_error();
+    if (!p || !d_proj || !d_workspace) return set_error(CTGB_ERR_ARG, "ctgb_integrate_projections: NULL argument");
+    if (nviews < 0 || nviews > p->nviews)
+        return set_error(CTGB_ERR_ARG, "ctgb_integrate_projections: view count %d outside [0,%d]", nviews, p->nviews);
+    const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    if (workspace_bytes < per_view * (size_t)nviews)
+        return set_error(CTGB_ERR_SIZE, "ctgb_integrate_projections: workspace below nviews views");
+    if (nviews == 0) return CTGB_OK;
+    const long long threads = (long long)p->nu * nviews;
+    integrate_rows_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        d_proj, static_cast<float2 *>(d_workspace), p->nu, p->nv, nviews);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "integrate_rows_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_backproject_fdk_integrated(const ctgb_params *p, const void *d_table, const void *d_integrated,
+                                               float *d_vol, int32_t view0, int32_t nviews, float scale,
+                                               int32_t accumulate, void *stream) {
+    clear_error();
+    int st = bp_args(p, d_table, static_cast<const float *>(d_integrated), d_vol, view0, nviews,
+                     "ctgb_backproject_fdk_integrated");
+    if (st) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nviews == 0) {
+        if (!accumulate) {
+            cudaError_t e = cudaMemsetAsync(d_vol, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nz, s);
+            if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
+        return CTGB_OK;
+    }
+    dim3 block(kBpTX, kBpTY);
+    dim3 grid((p->nx + kBpTX - 1) / kBpTX, (p->ny + kBpTY - 1) / kBpTY, (p->nz + kBiZ - 1) / kBiZ);
+    const float *T = static_cast<const float *>(d_table);
+    const float2 *ws = static_cast<const float2 *>(d_integrated);
+    if (p->curved)
+        bp_fdk_integ_kernel<true><<<grid, block, 0, s>>>(T, ws, d_vol, view0, nviews, scale, accumulate);
+    else
+        bp_fdk_integ_kernel<false><<<grid, block, 0, s>>>(T, ws, d_vol, view0, nviews, scale, accumulate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_integ_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;

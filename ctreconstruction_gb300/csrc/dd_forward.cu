@@ -518,6 +518,27 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
     return check_launch("dd_forward");
 }
 
+extern "C" int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_t nviews, int32_t *launches) {
+    clear_error();
+    if (!p || !launches) return set_error(CTGB_ERR_ARG, "ctgb_forward_launches: NULL argument");
+    if (view0 < 0 || nviews < 0 || view0 + nviews > p->nviews)
+        return set_error(CTGB_ERR_ARG, "ctgb_forward_launches: view range outside [0,%d)", p->nviews);
+    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + kTR - 1) / kTR;
+    const bool tiles_ok = (long long)ntu * ntv <= 65535;
+    std::vector<int> axes;
+    view_axes(p, view0, nviews, axes);
+    int count = 0;
+    for (int i = 0; i < nviews;) {
+        const int a = (axes[i] == 2 || !tiles_ok) ? 2 : axes[i];
+        int j = i + 1;
+        while (j < nviews && ((axes[j] == 2 || !tiles_ok) ? 2 : axes[j]) == a) ++j;
+        count += (j - i + 65534) / 65535;
+        i = j;
+    }
+    *launches = count;
+    return CTGB_OK;
+}
+
 extern "C" int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t ny, int32_t nz,
                                  void *stream) {
     clear_error();

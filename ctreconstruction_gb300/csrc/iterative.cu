@@ -5,6 +5,8 @@
 //   SART      python/SART.py:51,55
 //   MLEM      python/EM.py:36-42
 //   ASD-POCS  python/ASD_POCS.py:174-179 (POCS), :55-77 (tv_grad), :183,189 (norms)
+// The update passes may run in place (x_prev == x: each element is read, then
+// written, by the same thread), so those two pointers are not __restrict__.
 // All are HBM-bound streaming passes (grid-stride loops over 4-float
 // vectors where the arrays allow it).  Reductions are deterministic: each
 // block writes one double partial sum, and the consumer sums the partials in
@@ -33,8 +35,8 @@ __global__ void sart_residual_kernel(const float *__restrict__ ax, const float *
 }
 
 // SART.py:55  x = x_prev - alpha * (bp / norm1 + eps)   (eps added after the division, as written)
-__global__ void sart_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
-                                   const float *__restrict__ n1, float alpha, float eps, float *__restrict__ x,
+__global__ void sart_update_kernel(const float *xp, const float *__restrict__ bp,
+                                   const float *__restrict__ n1, float alpha, float eps, float *x,
                                    long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         x[i] = xp[i] - alpha * (bp[i] / n1[i] + eps);
@@ -53,8 +55,8 @@ __global__ void em_ratio_kernel(float *__restrict__ p0, const float *__restrict_
 }
 
 // EM.py:41-42  x = x_prev * (bp / norm)
-__global__ void em_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
-                                 const float *__restrict__ nrm, float *__restrict__ x, long long n) {
+__global__ void em_update_kernel(const float *xp, const float *__restrict__ bp,
+                                 const float *__restrict__ nrm, float *x, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         x[i] = xp[i] * (bp[i] / nrm[i]);
 }
@@ -70,8 +72,8 @@ __global__ void pocs_residual_kernel(const float *__restrict__ p0, const float *
 }
 
 // ASD_POCS.py:177-179  bp[norm1 == 0] = 0; x = x_prev + beta * bp / (norm1 + eps); x[x < 0] = 0
-__global__ void pocs_update_kernel(const float *__restrict__ xp, const float *__restrict__ bp,
-                                   const float *__restrict__ n1, float beta, float eps, float *__restrict__ x,
+__global__ void pocs_update_kernel(const float *xp, const float *__restrict__ bp,
+                                   const float *__restrict__ n1, float beta, float eps, float *x,
                                    long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {

@@ -68,52 +68,181 @@ def normalisers(P, matched=False):
     return norm1, norm2
 
 
-def sart(P, proj0, niter=10, alpha=1.0, eps=1e-5, x0=None, phantom=None, matched=False, norms=None):
-    """SART.py:44-59: x <- x - alpha * (B((Ax - p0) / (A1 + eps)) / norm1 + eps).
+class _Solver:
+    """An iterative solver whose device state (iterate, normalisers, scratch)
+    lives in tensors allocated once, so that one iteration is a fixed
+    sequence of stream-ordered launches: ``step()`` issues it eagerly,
+    ``capture()`` records it into a CUDA graph and ``run(n)`` replays that
+    graph n times (one graph launch per iteration)."""
 
-    Returns (x, rmse list).  x0 defaults to zeros, as in the script."""
-    P = P if isinstance(P, Projector) else Projector(P)
-    dev = P.device
-    S = _Scratch(P, dev)
-    norm1, norm2 = norms if norms is not None else normalisers(P, matched)
-    x = torch.zeros(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
-    xn = torch.empty_like(x)
-    rmse = []
-    n_p, n_v = _n(S.proj), _n(x)
-    for _ in range(niter):
-        P.forward(x, out=S.proj)
-        _lib.call("ctgb_sart_residual", _ptr(S.proj), _ptr(proj0), _ptr(norm2), eps, _ptr(S.res), n_p, _stream())
-        _backproject(P, S.res, S.bp, matched)
-        _lib.call("ctgb_sart_update", _ptr(x), _ptr(S.bp), _ptr(norm1), alpha, eps, _ptr(xn), n_v, _stream())
-        x, xn = xn, x
-        if phantom is not None:
-            rmse.append(_rmse(S, x, phantom))
-    return x, rmse
+    graph = None
+
+    def step(self):
+        raise NotImplementedError
+
+    def capture(self):
+        """Record one iteration into a CUDA graph.  Runs one eager iteration
+        first (it allocates the projectors' lazy buffers and sets kernel
+        attributes outside the capture) — the state advances by it."""
+        self.step()
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step()
+        self.graph = g
+        return g
+
+    def run(self, niter, phantom=None):
+        rmse = []
+        for _ in range(niter):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self.step()
+            if phantom is not None:
+                rmse.append(_rmse(self.S, self.x, phantom))
+        return rmse
+
+
+class SART(_Solver):
+    """SART.py:44-59: x <- x - alpha * (B((Ax - p0) / (A1 + eps)) / norm1 + eps).
+    x0 defaults to zeros, as in the script."""
+
+    def __init__(self, P, proj0, alpha=1.0, eps=1e-5, x0=None, matched=False, norms=None):
+        self.P = P if isinstance(P, Projector) else Projector(P)
+        self.device = dev = self.P.device
+        self.S = _Scratch(self.P, dev)
+        self.norm1, self.norm2 = norms if norms is not None else normalisers(self.P, matched)
+        self.proj0, self.alpha, self.eps, self.matched = proj0, float(alpha), float(eps), matched
+        self.x = torch.zeros(self.P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+
+    def step(self):
+        S, x = self.S, self.x
+        self.P.forward(x, out=S.proj)
+        _lib.call("ctgb_sart_residual", _ptr(S.proj), _ptr(self.proj0), _ptr(self.norm2), self.eps, _ptr(S.res),
+                  _n(S.proj), _stream())
+        _backproject(self.P, S.res, S.bp, self.matched)
+        # element-wise update, in place (each element reads only itself)
+        _lib.call("ctgb_sart_update", _ptr(x), _ptr(S.bp), _ptr(self.norm1), self.alpha, self.eps, _ptr(x), _n(x),
+                  _stream())
+
+
+class MLEM(_Solver):
+    """EM.py:32-44: x <- x * B(p0 / Ax) / B(1) with the script's zero guards.
+    proj0 is modified in place where Ax == 0 (the script's proj0 aliases its
+    measured data).  x0 defaults to ones, as in the script."""
+
+    def __init__(self, P, proj0, eps=1e-5, x0=None, matched=False, norm=None):
+        self.P = P if isinstance(P, Projector) else Projector(P)
+        self.device = dev = self.P.device
+        self.S = _Scratch(self.P, dev)
+        if norm is None:
+            norm = _backproject(self.P, torch.ones(self.P.proj_shape(), dtype=torch.float32, device=dev), None,
+                                matched)
+        self.norm, self.proj0, self.eps, self.matched = norm, proj0, float(eps), matched
+        self.x = torch.ones(self.P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+
+    def step(self):
+        S, x = self.S, self.x
+        self.P.forward(x, out=S.proj)
+        _lib.call("ctgb_em_ratio", _ptr(self.proj0), _ptr(S.proj), self.eps, _ptr(S.res), _n(S.proj), _stream())
+        _backproject(self.P, S.res, S.bp, self.matched)
+        _lib.call("ctgb_em_update", _ptr(x), _ptr(S.bp), _ptr(self.norm), _ptr(x), _n(x), _stream())
+
+
+class OSSART(_Solver):
+    """Ordered-subsets SART (no reference counterpart).
+
+    Subset s holds views s, s + nsubsets, s + 2 nsubsets, ... — itself a
+    regular scan (StartAngle + s * dtheta, the same angular span,
+    NumberOfViews / nsubsets views), so each subset gets its own Projector.
+    Each sub-iteration applies
+        x <- max(0, x + lam * B_s((p0_s - A_s x) / (A_s 1 + eps)) / (B_s 1 + eps))
+    with rows/voxels whose normaliser is zero left untouched; one step() is
+    one pass over all subsets."""
+
+    def __init__(self, P, proj0, nsubsets=10, lam=0.8, eps=1e-5, x0=None, matched=True):
+        P = P if isinstance(P, Projector) else Projector(P)
+        self.P, self.device = P, P.device
+        dev = P.device
+        base = P.params
+        nv = base.NumberOfViews
+        if nsubsets < 1 or nv % nsubsets:
+            raise ValueError("NumberOfViews (%d) must be divisible by nsubsets (%d)" % (nv, nsubsets))
+        span = base.EndAngle - base.StartAngle
+        dth = span / nv
+        vol_ones = torch.ones(P.volume_shape, dtype=torch.float32, device=dev)
+        self.subsets = []
+        for s in range(nsubsets):
+            d = base.as_dict()
+            d['StartAngle'] = base.StartAngle + s * dth
+            d['EndAngle'] = d['StartAngle'] + span
+            d['NumberOfViews'] = nv // nsubsets
+            Ps = Projector(ReconstructionParams.from_dict(d, base.flavour), device=dev)
+            ps0 = proj0[s::nsubsets].contiguous()
+            a1 = Ps.forward(vol_ones)
+            b1 = _backproject(Ps, torch.ones_like(ps0), None, matched)
+            self.subsets.append((Ps, ps0, a1, b1))
+        self.x = torch.zeros(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
+        self.S = _Scratch(self.subsets[0][0], dev)
+        self.lam, self.eps, self.matched = float(lam), float(eps), matched
+
+    def step(self):
+        S, x = self.S, self.x
+        for Ps, ps0, a1, b1 in self.subsets:
+            Ps.forward(x, out=S.proj)
+            _lib.call("ctgb_pocs_residual", _ptr(ps0), _ptr(S.proj), _ptr(a1), self.eps, _ptr(S.res), _n(S.res),
+                      _stream())
+            _backproject(Ps, S.res, S.bp, self.matched)
+            _lib.call("ctgb_pocs_update", _ptr(x), _ptr(S.bp), _ptr(b1), self.lam, self.eps, _ptr(x), _n(x),
+                      _stream())
+
+
+class SolverBatch:
+    """Many solvers (scans of uneven sizes) advanced together: one CUDA graph
+    holds one iteration of every solver, so a batch iteration is a single
+    graph launch."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        self.device = self.solvers[0].device
+        self.graph = None
+
+    def step(self):
+        for s in self.solvers:
+            s.step()
+
+    def capture(self):
+        self.step()
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step()
+        self.graph = g
+        return g
+
+    def run(self, niter):
+        for _ in range(niter):
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self.step()
+
+
+def sart(P, proj0, niter=10, alpha=1.0, eps=1e-5, x0=None, phantom=None, matched=False, norms=None, graph=False):
+    """SART.py:44-59; returns (x, rmse list)."""
+    s = SART(P, proj0, alpha, eps, x0, matched, norms)
+    if graph and niter > 0:
+        x_start = s.x.clone()
+        s.capture()                 # advances the state by one (eager warm-up) iteration
+        s.x.copy_(x_start)
+    return s.x, s.run(niter, phantom)
 
 
 def mlem(P, proj0, niter=10, eps=1e-5, x0=None, phantom=None, matched=False, norm=None):
-    """EM.py:32-44: x <- x * B(p0 / Ax) / B(1) with the script's zero guards.
-
-    proj0 is modified in place where Ax == 0 (the script's proj0 aliases its
-    measured data).  x0 defaults to ones, as in the script."""
-    P = P if isinstance(P, Projector) else Projector(P)
-    dev = P.device
-    S = _Scratch(P, dev)
-    if norm is None:
-        norm = _backproject(P, torch.ones(P.proj_shape(), dtype=torch.float32, device=dev), None, matched)
-    x = torch.ones(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
-    xn = torch.empty_like(x)
-    rmse = []
-    n_p, n_v = _n(S.proj), _n(x)
-    for _ in range(niter):
-        P.forward(x, out=S.proj)
-        _lib.call("ctgb_em_ratio", _ptr(proj0), _ptr(S.proj), eps, _ptr(S.res), n_p, _stream())
-        _backproject(P, S.res, S.bp, matched)
-        _lib.call("ctgb_em_update", _ptr(x), _ptr(S.bp), _ptr(norm), _ptr(xn), n_v, _stream())
-        x, xn = xn, x
-        if phantom is not None:
-            rmse.append(_rmse(S, x, phantom))
-    return x, rmse
+    """EM.py:32-44; returns (x, rmse list)."""
+    s = MLEM(P, proj0, eps, x0, matched, norm)
+    return s.x, s.run(niter, phantom)
 
 
 def tv_descent(x, step, ng, eps=1e-7):
@@ -180,45 +309,6 @@ def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.
 
 
 def os_sart(P, proj0, nsubsets=10, niter=20, lam=0.8, eps=1e-5, x0=None, phantom=None, matched=True):
-    """Ordered-subsets SART (no reference counterpart).
-
-    Subset s holds views s, s + nsubsets, s + 2 nsubsets, ... — itself a
-    regular scan (StartAngle + s * dtheta, the same angular span,
-    NumberOfViews / nsubsets views), so each subset gets its own Projector.
-    Each sub-iteration applies
-        x <- max(0, x + lam * B_s((p0_s - A_s x) / (A_s 1 + eps)) / (B_s 1 + eps))
-    with rows/voxels whose normaliser is zero left untouched."""
-    P = P if isinstance(P, Projector) else Projector(P)
-    dev = P.device
-    base = P.params
-    nv = base.NumberOfViews
-    if nsubsets < 1 or nv % nsubsets:
-        raise ValueError("NumberOfViews (%d) must be divisible by nsubsets (%d)" % (nv, nsubsets))
-    span = base.EndAngle - base.StartAngle
-    step = span / nv
-    vol_ones = torch.ones(P.volume_shape, dtype=torch.float32, device=dev)
-    subsets = []
-    for s in range(nsubsets):
-        d = base.as_dict()
-        d['StartAngle'] = base.StartAngle + s * step
-        d['EndAngle'] = d['StartAngle'] + span
-        d['NumberOfViews'] = nv // nsubsets
-        Ps = Projector(ReconstructionParams.from_dict(d, base.flavour), device=dev)
-        ps0 = proj0[s::nsubsets].contiguous()
-        a1 = Ps.forward(vol_ones)
-        b1 = _backproject(Ps, torch.ones_like(ps0), None, matched)
-        subsets.append((Ps, ps0, a1, b1))
-    x = torch.zeros(P.volume_shape, dtype=torch.float32, device=dev) if x0 is None else x0.clone()
-    S = _Scratch(subsets[0][0], dev)
-    n_v = _n(x)
-    rmse = []
-    for _ in range(niter):
-        for Ps, ps0, a1, b1 in subsets:
-            Ps.forward(x, out=S.proj)
-            _lib.call("ctgb_pocs_residual", _ptr(ps0), _ptr(S.proj), _ptr(a1), eps, _ptr(S.res), _n(S.res),
-                      _stream())
-            _backproject(Ps, S.res, S.bp, matched)
-            _lib.call("ctgb_pocs_update", _ptr(x), _ptr(S.bp), _ptr(b1), lam, eps, _ptr(x), n_v, _stream())
-        if phantom is not None:
-            rmse.append(_rmse(S, x, phantom))
-    return x, rmse
+    """OSSART run for niter passes; returns (x, rmse list)."""
+    s = OSSART(P, proj0, nsubsets, lam, eps, x0, matched)
+    return s.x, s.run(niter, phantom)

@@ -105,6 +105,43 @@ class Projector:
                       view0, nviews, sc, int(bool(accumulate)), _ptr(ws), ws.numel() * 4, _stream())
         return out
 
+    def forward_launches(self, view0=0, nviews=None):
+        """Kernel launches one forward() call makes over this view range."""
+        view0, nviews = self._views(view0, nviews)
+        n = ctypes.c_int32(0)
+        _lib.call("ctgb_forward_launches", ctypes.byref(self.c), view0, nviews, ctypes.byref(n))
+        return n.value
+
+    def integrate(self, proj, nviews=None, out=None):
+        """Integrated projections of the first nviews views of proj (running
+        sum along v, value) as the float2 workspace the FDK backprojector
+        reads; returns the workspace tensor (flat float32)."""
+        nviews = self.params.NumberOfViews if nviews is None else int(nviews)
+        self._check(proj, self.proj_shape(nviews), "proj")
+        n = ctypes.c_size_t(0)
+        _lib.call("ctgb_backproject_fdk_workspace_bytes", ctypes.byref(self.c), nviews, ctypes.byref(n))
+        if out is None or out.numel() * 4 < n.value:
+            out = torch.empty((n.value + 3) // 4, dtype=torch.float32, device=proj.device)
+        _lib.call("ctgb_integrate_projections", ctypes.byref(self.c), _ptr(proj), nviews, _ptr(out), out.numel() * 4,
+                  _stream())
+        return out
+
+    def backproject_fdk_integrated(self, integrated, out=None, view0=0, nviews=None, scale=None, accumulate=False):
+        """backproject_fdk from projections already integrated by integrate()."""
+        view0, nviews = self._views(view0, nviews)
+        if out is None:
+            out = torch.empty(self.volume_shape, dtype=torch.float32, device=integrated.device)
+            accumulate = False
+        self._check(out, self.volume_shape, "out")
+        n = ctypes.c_size_t(0)
+        _lib.call("ctgb_backproject_fdk_workspace_bytes", ctypes.byref(self.c), nviews, ctypes.byref(n))
+        if integrated.numel() * 4 < n.value or integrated.dtype != torch.float32 or not integrated.is_cuda:
+            raise ValueError("integrated: need a CUDA float32 tensor of at least %d bytes" % n.value)
+        sc = self.params.dtheta if scale is None else float(scale)
+        _lib.call("ctgb_backproject_fdk_integrated", ctypes.byref(self.c), _ptr(self.table), _ptr(integrated),
+                  _ptr(out), view0, nviews, sc, int(bool(accumulate)), _stream())
+        return out
+
     # Integrated-projection workspace of the FDK backprojector: all views when
     # that fits in WORKSPACE_CAP bytes, else chunks of views.
     WORKSPACE_CAP = 6 << 30

@@ -70,6 +70,9 @@ int ctgb_table_build(const ctgb_params *p, void *host_table, size_t bytes);
  * overwritten.  Stream-ordered; no synchronisation. */
 int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                  float *d_proj, int32_t view0, int32_t nviews, void *stream);
+/* Number of kernel launches ctgb_forward makes for this view range (one per
+ * run of consecutive views with the same dominant axis). */
+int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_t nviews, int32_t *launches);
 
 /* Same result as ctgb_forward, for callers that cannot allocate device
  * memory where they project (an application whose own pool owns the device
@@ -107,6 +110,18 @@ int ctgb_backproject_fdk_workspace_bytes(const ctgb_params *p, int32_t nviews, s
 int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                             int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
                             size_t workspace_bytes, void *stream);
+/* The two stages of ctgb_backproject_fdk_ws as separate calls, so that one
+ * set of integrated projections can serve several backprojections (and each
+ * stage can be timed alone): ctgb_integrate_projections writes nviews views
+ * of d_proj as (running sum, value) pairs into d_workspace (at least
+ * ctgb_backproject_fdk_workspace_bytes(p, nviews) bytes);
+ * ctgb_backproject_fdk_integrated backprojects nviews integrated views
+ * (geometry of views view0 .. view0+nviews-1) from there. */
+int ctgb_integrate_projections(const ctgb_params *p, const float *d_proj, int32_t nviews, void *d_workspace,
+                               size_t workspace_bytes, void *stream);
+int ctgb_backproject_fdk_integrated(const ctgb_params *p, const void *d_table, const void *d_integrated,
+                                    float *d_vol, int32_t view0, int32_t nviews, float scale, int32_t accumulate,
+                                    void *stream);
 
 /* ---- matched DD backprojection (exact adjoint of ctgb_forward) -------------
  * No reference counterpart (the reference's backward() is FDK-weighted);
@@ -200,6 +215,42 @@ int ctgb_fan_batch_build(const ctgb_fan_slice *slices, int32_t nslices, int32_t 
  * threads (the tile the batch was built with); max_views >= every slice's nviews. */
 int ctgb_fan_backproject(const void *d_batch, int32_t max_views, const float *d_sino, float *d_images,
                          int32_t tile_x, int32_t tile_y, int32_t grid_blocks, int32_t accumulate, void *stream);
+
+/* ---- iterative update passes ------------------------------------------------
+ * Element-wise float32 passes over n elements of device arrays, one per
+ * update line of the reference drivers (the A / A^T products come from
+ * ctgb_forward / ctgb_backproject_*):
+ *   ctgb_sart_residual  out = (ax - p0) / (a1 + eps)            python/SART.py:51
+ *   ctgb_sart_update    x = x_prev - alpha * (bp / norm1 + eps) python/SART.py:55
+ *   ctgb_em_ratio       p0[ax == 0] = 0 (in place); ax -> eps where 0; out = p0 / ax
+ *                                                               python/EM.py:36-39
+ *   ctgb_em_update      x = x_prev * (bp / norm)                python/EM.py:41-42
+ *   ctgb_pocs_residual  out = (p0 - ax) / (a1 + eps), 0 where a1 == 0
+ *                                                               python/ASD_POCS.py:174-175
+ *   ctgb_pocs_update    x = max(0, x_prev + beta * bp / (norm1 + eps)), bp -> 0 where norm1 == 0
+ *                                                               python/ASD_POCS.py:177-179
+ *   ctgb_tv_step        y = x - step * g / ||g|| with g = tv_grad(x) on the
+ *                       interior of the [n0][n1][n2] array (python/ASD_POCS.py:55-77,
+ *                       :186-189); y's border is x's; x != y.
+ *   ctgb_sqdist         out[0] = sum (a - b)^2 (b may be NULL: sum a^2), as double
+ *                       (the norms of python/ASD_POCS.py:183,189).
+ * The update passes accept x == x_prev (in place).  Reductions are
+ * deterministic: `partials` holds ctgb_partials_count(n) doubles, one per
+ * block, summed in a fixed order. */
+int ctgb_partials_count(int64_t n, int32_t *count);
+int ctgb_sart_residual(const float *ax, const float *p0, const float *a1, float eps, float *out, int64_t n,
+                       void *stream);
+int ctgb_sart_update(const float *x_prev, const float *bp, const float *norm1, float alpha, float eps, float *x,
+                     int64_t n, void *stream);
+int ctgb_em_ratio(float *p0, const float *ax, float eps, float *out, int64_t n, void *stream);
+int ctgb_em_update(const float *x_prev, const float *bp, const float *norm, float *x, int64_t n, void *stream);
+int ctgb_pocs_residual(const float *p0, const float *ax, const float *a1, float eps, float *out, int64_t n,
+                       void *stream);
+int ctgb_pocs_update(const float *x_prev, const float *bp, const float *norm1, float beta, float eps, float *x,
+                     int64_t n, void *stream);
+int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, int32_t n2, float eps, float step,
+                 double *partials, void *stream);
+int ctgb_sqdist(const float *a, const float *b, int64_t n, double *partials, double *out, void *stream);
 
 /* ---- status ----------------------------------------------------------------
  * ctgb_device_status: the device-side status word of the current device

@@ -130,3 +130,17 @@ def test_product_never_imports_the_oracle():
             if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
                 text = open(os.path.join(root, f)).read()
                 assert "import oracle" not in text and "from oracle" not in text, f
+
+
+def test_forward_launch_count():
+    """ctgb_forward_launches counts runs of same-axis views: a full circle
+    from theta 0 alternates y, x, y, x, y dominant views (host-only call)."""
+    p = cone_params(n=16, nviews=360, nu=32, nv=24, start=0.0, span=2 * np.pi)
+    c = ReconstructionParams.from_dict(p).to_ctgb()
+    n = ctypes.c_int32(0)
+    _lib.call("ctgb_forward_launches", ctypes.byref(c), 0, 360, ctypes.byref(n))
+    assert n.value == 5
+    _lib.call("ctgb_forward_launches", ctypes.byref(c), 0, 10, ctypes.byref(n))
+    assert n.value == 1
+    with pytest.raises(ValueError):
+        _lib.call("ctgb_forward_launches", ctypes.byref(c), 350, 20, ctypes.byref(n))

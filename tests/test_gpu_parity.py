@@ -198,3 +198,11 @@ def test_fdk_backprojector_entry_points_agree(cuda, gname):
               ctypes.c_void_p(ws.data_ptr()), n.value, stream)
     assert rel_err(a.cpu().numpy(), want) < RTOL
     assert rel_err(b.cpu().numpy(), want) < RTOL
+    # the two stages as separate calls: same kernels, same bits as the chunked
+    # path when one chunk holds every view
+    integ = P.integrate(yt)
+    c = P.backproject_fdk_integrated(integ)
+    d = P.backproject_fdk(yt)
+    assert torch.equal(c, d)
+    assert rel_err(c.cpu().numpy(), want) < RTOL
+
