@@ -333,7 +333,8 @@ def run_ours(args):
                            "views": nviews, "detector": [P.params.nu, P.params.nv], "voxel_mm": 0.5,
                            "pixel_mm": 0.75, "sad_mm": 1000, "sdd_mm": 1500,
                            "step": "forward() + backward() (DD forward, FDK-weighted DD backprojection)",
-                           "l2": "inputs larger than L2 (volume 512 MiB, projections 2.16 GiB)",
+                           "l2": "inputs larger than L2 (volume %.0f MiB, projections %.2f GiB)" % (
+                               4.0 * n ** 3 / 2 ** 20, 4.0 * proj.numel() / 2 ** 30),
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "kernels_ms": kern, "gpu_launches": launches_per_step * args.steps, "effective_hbm_gbs": 2 * 4 * vv / (ms / 1e3) / 1e9,
                 "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks, "matched_pair": matched}
