@@ -30,7 +30,6 @@
 #include "dd_common.cuh"
 #include "status.h"
 #include "tma.cuh"
-#include "f32x2.cuh"
 
 namespace ctgb {
 
@@ -234,7 +233,7 @@ bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj,
 // each lookup carries one float32 rounding of the prefix, not a drifting sum.
 constexpr int kBiZ = 16;
 #ifndef CTGB_BI_BLOCKS
-#define CTGB_BI_BLOCKS 5
+#define CTGB_BI_BLOCKS 6
 #endif
 constexpr int kBiBlocks = CTGB_BI_BLOCKS;   // resident CTAs per SM the register budget is sized for
 
@@ -269,21 +268,12 @@ __device__ __forceinline__ float integ_taps(const float2 *__restrict__ rlo, cons
 // CLAMP: some footprint of the chunk may leave the detector's rows [0, nv];
 // without it every footprint lies inside (checked per warp by the caller),
 // and every footprint is at least 1e-4 rows wide (also checked).
-//
-// The (lo, hi) ends of a voxel's footprint travel as one f32x2 pair through
-// the floor/fraction split, and each tap's (C, Q) float2 is accumulated as a
-// pair: SL = sum_t ov_t (C, Q)(lo row), SH likewise at the hi row, so the
-// footprint integral is (SH.C + uhi SH.Q) - (SL.C + ulo SL.Q).
 template <int NT, bool LINEAR, bool CLAMP>
 __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int nu, int nv, int lbase,
                                              const float *ov, float lo0, float hi0, float dlo, float dhi,
                                              float zfirst, float dzs, float hz, float Sz, float imin, float imax,
                                              float Mv, float Av, float wscale, float *acc) {
     const float fnv = (float)nv;
-    const f2x magic = f2_pack(12582912.0f, 12582912.0f);
-    f2x ovp[NT];
-#pragma unroll
-    for (int t = 0; t < NT; ++t) ovp[t] = f2_pack(ov[t], ov[t]);
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) {
         float vlo, vhi;
@@ -298,25 +288,17 @@ __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int 
             vlo = fminf(fmaxf(vlo, 0.0f), fnv);
             vhi = fminf(fmaxf(vhi, 0.0f), fnv);
         }
-        const f2x vp = f2_pack(vlo, vhi);
-        const f2x tp = f2_add_rd(vp, magic);            // floor_split on both ends
-        const f2x up = f2_sub(vp, f2_sub(tp, magic));   // (ulo, uhi) fractions
-        float tlo, thi, ulo, uhi;
-        f2_unpack(tp, tlo, thi);
-        f2_unpack(up, ulo, uhi);
-        const int mlo = __float_as_int(tlo) - 0x4B400000, mhi = __float_as_int(thi) - 0x4B400000;
+        float flo, fhi;
+        const int mlo = floor_split(vlo, &flo), mhi = floor_split(vhi, &fhi);
         const float2 *rlo = IQ + mlo * nu + lbase;
         const float2 *rhi = IQ + mhi * nu + lbase;
-        f2x sl = f2_mul(ovp[0], f2_ldg(rlo)), sh = f2_mul(ovp[0], f2_ldg(rhi));
+        const float ulo = vlo - flo, uhi = vhi - fhi;
+        float s = 0.0f;
 #pragma unroll
-        for (int t = 1; t < NT; ++t) {
-            sl = f2_fma(ovp[t], f2_ldg(rlo + t), sl);
-            sh = f2_fma(ovp[t], f2_ldg(rhi + t), sh);
+        for (int t = 0; t < NT; ++t) {
+            const float2 a = __ldg(rlo + t), b = __ldg(rhi + t);
+            s = fmaf(ov[t], fmaf(b.y, uhi, b.x) - fmaf(a.y, ulo, a.x), s);
         }
-        float slc, slq, shc, shq;
-        f2_unpack(sl, slc, slq);
-        f2_unpack(sh, shc, shq);
-        const float s = fmaf(uhi, shq, shc) - fmaf(ulo, slq, slc);
         acc[j] = fmaf(s * rw, wscale, acc[j]);
     }
 }
