@@ -61,6 +61,19 @@ SIGNATURES = {
     "ctgb_backproject_matched_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],
     "ctgb_integrate_projections": [_P, _vp, _i32, _vp, _sz, _vp],
     "ctgb_forward_launches": [_P, _i32, _i32, ctypes.POINTER(_i32)],
+    "ctgb_unet_conv3d": [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_input": [_vp, _vp, _vp, _i32, ctypes.c_int64, _vp],
+    "ctgb_unet_pool2": [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_up2": [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_relu_grad": [_vp, _i32, _i32, _vp, _vp, ctypes.c_int64, _i32, _vp],
+    "ctgb_unet_pool2_grad": [_vp, _vp, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_up2_grad": [_vp, _i32, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_head": [_vp, _vp, _vp, _vp, _vp, _i32, ctypes.c_int64, _vp],
+    "ctgb_unet_head_grad_blocks": [ctypes.c_int64, ctypes.POINTER(_i32)],
+    "ctgb_unet_head_grad": [_vp, _vp, _vp, _vp, _vp, _vp, _i32, ctypes.c_int64, _vp],
+    "ctgb_unet_wgrad_chunks": [_i32, _i32, _i32, _i32, ctypes.POINTER(_i32)],
+    "ctgb_unet_wgrad": [_vp, _i32, _vp, _i32, _vp, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_unet_colsum": [_vp, _i32, ctypes.c_int64, _vp, _i32, _vp],
     "ctgb_backproject_fdk_integrated": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_filter_bytes": [_P, ctypes.POINTER(_sz)],
     "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],

@@ -166,31 +166,36 @@ struct PatchCells {
     }
 };
 
-// Integrate h over consecutive row boundaries of one chain of N rows.  MID:
-// a row may cover three cells (one whole cell in the middle); rows never
-// cover four (checked per slice by the caller).  No data-dependent branches.
+// Integrate h over consecutive row boundaries of two chains of N rows (rows
+// 0..N-1 and N..2N-1), stepped together so that each chain's floor/lookup
+// latency overlaps the other's.  MID: a row may cover three cells (one whole
+// cell in the middle); rows never cover four (checked per slice by the
+// caller).  No data-dependent branches.
 template <int NT, bool MID, int N>
-__device__ __forceinline__ void sweep_rows(const PatchCells<NT> &H, const float *Bj, float A, float tau, float g,
-                                           float *acc) {
-    float f0;
-    const float z0 = fmaf(Bj[0], tau, A);
-    int m0 = floor_split(z0, &f0);
-    float h0 = H(m0);
-    float e0 = h0 * (z0 - f0);
+__device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float *Bj, float A, float tau, float g,
+                                            float *acc) {
+    float f0a, f0b;
+    const float z0a = fmaf(Bj[0], tau, A), z0b = fmaf(Bj[N], tau, A);
+    int m0a = floor_split(z0a, &f0a), m0b = floor_split(z0b, &f0b);
+    float h0a = H(m0a), h0b = H(m0b);
+    float e0a = h0a * (z0a - f0a), e0b = h0b * (z0b - f0b);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        float f1;
-        const float z1 = fmaf(Bj[j + 1], tau, A);
-        const int m1 = floor_split(z1, &f1);
-        const float h1 = H(m1);
-        const float e1 = h1 * (z1 - f1);
-        float whole = (m1 > m0) ? h0 : 0.0f;
+        float f1a, f1b;
+        const float z1a = fmaf(Bj[j + 1], tau, A), z1b = fmaf(Bj[N + j + 1], tau, A);
+        const int m1a = floor_split(z1a, &f1a), m1b = floor_split(z1b, &f1b);
+        const float h1a = H(m1a), h1b = H(m1b);
+        const float e1a = h1a * (z1a - f1a), e1b = h1b * (z1b - f1b);
+        float wa = (m1a > m0a) ? h0a : 0.0f, wb = (m1b > m0b) ? h0b : 0.0f;
         if (MID) {
-            const float hm = H(m0 + 1);
-            whole += (m1 > m0 + 1) ? hm : 0.0f;
+            const float hma = H(m0a + 1), hmb = H(m0b + 1);
+            wa += (m1a > m0a + 1) ? hma : 0.0f;
+            wb += (m1b > m0b + 1) ? hmb : 0.0f;
         }
-        acc[j] = fmaf(whole + e1 - e0, g, acc[j]);
-        m0 = m1; h0 = h1; e0 = e1;
+        acc[j] = fmaf(wa + e1a - e0a, g, acc[j]);
+        acc[N + j] = fmaf(wb + e1b - e0b, g, acc[N + j]);
+        m0a = m1a; h0a = h1a; e0a = e1a;
+        m0b = m1b; h0b = h1b; e0b = e1b;
     }
 }
 
@@ -201,8 +206,7 @@ __device__ __forceinline__ void sweep_tile(const float *patch, int lb, const flo
     H.base = patch;
     H.lb = lb;
     H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
-    sweep_rows<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
-    sweep_rows<NT, MID, kTR / 2>(H, Bj + kTR / 2, A, tau, g, acc + kTR / 2);
+    sweep_rows2<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
 }
 
 template <bool XD, bool TMA>

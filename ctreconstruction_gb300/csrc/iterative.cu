@@ -104,25 +104,71 @@ __device__ __forceinline__ float tv_term(const float *__restrict__ x, int n1, in
     return t1 + t2 + t3 + t4;
 }
 
-// Pass 1: per-block partial sums of dtv^2 over the interior.
+// Pass 1: per-block partial sums of dtv^2 over the interior.  Each warp
+// walks whole rows (i, j) of the array (rows distributed grid-stride over the
+// block's warps), its lanes striding along k, so the only integer division
+// is one 32-bit split of the row index per row.
 __global__ void tv_norm_kernel(const float *__restrict__ x, int n0, int n1, int n2, float eps,
                                double *__restrict__ partials) {
     __shared__ double red[kEwThreads / 32];
-    const long long m0 = n0 - 2, m1 = n1 - 2, m2 = n2 - 2, tot = m0 * m1 * m2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const unsigned m1 = (unsigned)(n1 - 2), rows = (unsigned)(n0 - 2) * m1;
     double acc = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(t % m2) + 1, j = (int)((t / m2) % m1) + 1, i = (int)(t / (m1 * m2)) + 1;
-        const float d = tv_term(x, n1, n2, i, j, k, eps);
-        acc += (double)d * d;
+    for (unsigned r = blockIdx.x * wpb + warp; r < rows; r += gridDim.x * wpb) {
+        const int i = (int)(r / m1) + 1, j = (int)(r % m1) + 1;
+        float racc = 0.0f;
+        for (int k = 1 + lane; k < n2 - 1; k += 32) {
+            const float d = tv_term(x, n1, n2, i, j, k, eps);
+            racc = fmaf(d, d, racc);
+        }
+        acc += (double)racc;
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    if (lane == 0) red[warp] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
-        for (int w = 0; w < kEwThreads / 32; ++w) s += red[w];
+        for (int w = 0; w < wpb; ++w) s += red[w];
         partials[blockIdx.x] = s;
+    }
+}
+
+// Pass 1b: partials[0] = sum of partials[0 .. np-1] (one block, fixed order:
+// per-thread strided sums, then a tree).
+constexpr int kReduceThreads = 1024;
+
+__global__ void __launch_bounds__(kReduceThreads) reduce_partials_kernel(double *partials, int np) {
+    __shared__ double red[kReduceThreads];
+    double s = 0.0;
+    for (int b = threadIdx.x; b < np; b += kReduceThreads) s += partials[b];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kReduceThreads / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[0] = red[0];
+}
+
+// Pass 2: y = x - step * dtv / ||dtv|| (||dtv|| -> 1 when below eps), with
+// ||dtv||^2 in partials[0]; the border of y is x's border (tv_grad pads dtv
+// with zeros).  Rows as in pass 1.
+__global__ void tv_step_kernel(const float *__restrict__ x, float *__restrict__ y, int n0, int n1, int n2, float eps,
+                               const double *__restrict__ partials, float step) {
+    float nrm = (float)sqrt(partials[0]);
+    if (fabsf(nrm) < eps) nrm = 1.0f;
+    const float inv = 1.0f / nrm;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    const unsigned rows = (unsigned)n0 * (unsigned)n1;
+    for (unsigned r = blockIdx.x * wpb + warp; r < rows; r += gridDim.x * wpb) {
+        const int i = (int)(r / (unsigned)n1), j = (int)(r % (unsigned)n1);
+        const long long base = (long long)r * n2;
+        const bool inner_row = i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
+        for (int k = lane; k < n2; k += 32) {
+            float v = x[base + k];
+            if (inner_row && k > 0 && k < n2 - 1) v = v - step * (tv_term(x, n1, n2, i, j, k, eps) * inv);
+            y[base + k] = v;
+        }
     }
 }
 
@@ -130,29 +176,6 @@ __device__ __forceinline__ double sum_partials(const double *__restrict__ partia
     double s = 0.0;
     for (int b = 0; b < np; ++b) s += partials[b];
     return s;
-}
-
-// Pass 2: y = x - step * dtv / ||dtv|| (||dtv|| -> 1 when below eps); the
-// border of y is x's border (tv_grad pads dtv with zeros).
-__global__ void tv_step_kernel(const float *__restrict__ x, float *__restrict__ y, int n0, int n1, int n2, float eps,
-                               const double *__restrict__ partials, int np, float step) {
-    __shared__ float s_inv;
-    if (threadIdx.x == 0) {
-        float nrm = (float)sqrt(sum_partials(partials, np));
-        if (fabsf(nrm) < eps) nrm = 1.0f;
-        s_inv = 1.0f / nrm;
-    }
-    __syncthreads();
-    const float inv = s_inv;
-    const long long tot = (long long)n0 * n1 * n2;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(t % n2), j = (int)((t / n2) % n1), i = (int)(t / ((long long)n1 * n2));
-        float v = x[t];
-        if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1)
-            v = v - step * (tv_term(x, n1, n2, i, j, k, eps) * inv);
-        y[t] = v;
-    }
 }
 
 // Per-block partial sums of (a - b)^2 (b may be NULL: sum of a^2).
@@ -278,7 +301,8 @@ extern "C" int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, in
         return CTGB_OK;
     }
     tv_norm_kernel<<<nb, kEwThreads, 0, st>>>(x, n0, n1, n2, eps, partials);
-    tv_step_kernel<<<nb, kEwThreads, 0, st>>>(x, y, n0, n1, n2, eps, partials, nb, step);
+    reduce_partials_kernel<<<1, kReduceThreads, 0, st>>>(partials, nb);
+    tv_step_kernel<<<nb, kEwThreads, 0, st>>>(x, y, n0, n1, n2, eps, partials, step);
     return launched("ctgb_tv_step");
 }
 

@@ -51,6 +51,34 @@ bool ctgb_make_tmap_3d(CUtensorMap *map, const float *base, const uint64_t dims[
     return r == CUDA_SUCCESS;
 }
 
+bool ctgb_make_tmap_bf16(CUtensorMap *map, const void *base, int rank, const uint64_t *dims, const uint32_t *box) {
+    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+    if (!fn || rank < 1 || rank > 5) return false;
+    cuuint64_t gdim[5], gstride[4];
+    cuuint32_t bdim[5], estride[5];
+    uint64_t stride = 2;
+    for (int i = 0; i < rank; ++i) {
+        gdim[i] = dims[i];
+        bdim[i] = box[i];
+        estride[i] = 1;
+        if (i > 0) gstride[i - 1] = stride;
+        stride *= dims[i];
+    }
+    for (int i = 0; i + 1 < rank; ++i)
+        if (gstride[i] % 16) return false;
+    if (reinterpret_cast<uintptr_t>(base) % 16) return false;
+    const uint32_t inner = box[0] * 2;
+    CUtensorMapSwizzle sw;
+    if (inner == 32) sw = CU_TENSOR_MAP_SWIZZLE_32B;
+    else if (inner == 64) sw = CU_TENSOR_MAP_SWIZZLE_64B;
+    else if (inner == 128) sw = CU_TENSOR_MAP_SWIZZLE_128B;
+    else return false;
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void *>(base), gdim, gstride,
+                    bdim, estride, CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // Reads (and optionally clears) the device status word of the current device.
 // Synchronises the device.  *out = 0 when no kernel reported a problem.
 extern "C" int ctgb_device_status(int32_t *out, int32_t clear) {

@@ -75,6 +75,11 @@ __device__ __forceinline__ int floor_split(float x, float *f) {
 // Returns false if the driver rejects the description (e.g. unaligned strides).
 bool ctgb_make_tmap_3d(CUtensorMap *map, const float *base, const uint64_t dims[3], const uint32_t box[3]);
 
+// Host: a bf16 tiled tensor map of `rank` dims (innermost first, dense
+// strides), with the shared-memory swizzle whose span equals the box's inner
+// extent in bytes (32, 64 or 128).  Out-of-bounds elements load as zeros.
+bool ctgb_make_tmap_bf16(CUtensorMap *map, const void *base, int rank, const uint64_t *dims, const uint32_t *box);
+
 // Host: device address of the library's status word on the current device
 // (a file-scope __device__ int in runtime.cu; looked up once per device).
 int *ctgb_status_ptr();

@@ -1,0 +1,691 @@
+// Learned proximal step: the building blocks of a small 3-D U-Net (no
+// reference counterpart; it stands in for ASD-POCS's TV descent,
+// python/ASD_POCS.py:186-190).
+//
+// Activations are bf16 in [N][D][H][W][C] order (channels innermost, C in
+// {16, 32, 64}); weights of a 3x3x3 convolution are [27 taps][Cout][Cin]
+// (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)); accumulation is fp32.
+//
+// conv3d_tc_kernel is an implicit GEMM on the 5th-generation tensor cores:
+// one CTA computes a tile of M = 128 output voxels x Cout channels.  The K
+// loop runs over the 27 taps (x the input segments of a channel concat):
+// per step TMA brings the 128 shifted input voxels (a box {C, Wb, R, 1, 1} of
+// the 5-D activation tensor; zero fill outside the volume is the conv's zero
+// padding) and the tap's [Cout][C] weight block into a 4-stage ring of
+// shared-memory buffers, in the swizzled K-major layout tcgen05 reads; one
+// thread issues tcgen05.mma (M = 128, N = Cout, K = 16 per instruction)
+// into a TMEM accumulator, and tcgen05.commit releases each stage.  The
+// epilogue reads TMEM with tcgen05.ld (one row per thread), adds the bias,
+// applies ReLU and stores bf16 — or stores the raw fp32 sums (the data
+// gradient, which runs the same kernel on flipped weights).
+//
+// The remaining passes (input packing, pooling, upsampling, masks, the 1x1
+// head, the weight gradient) are CUDA-core kernels.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/ctgb.h"
+#include "status.h"
+#include "tcgen05.cuh"
+#include "tma.cuh"
+
+namespace ctgb {
+
+constexpr int kCvM = 128, kCvThreads = 128;
+
+template <int COUT>
+struct ConvCfg {
+    static constexpr int kABytes = kCvM * 128;                          // 128 rows of up to 128 B
+    static constexpr int kBBytes = ((COUT * 128 + 1023) / 1024) * 1024;  // COUT rows of up to 128 B
+    static constexpr int kStage = kABytes + kBBytes;
+    static constexpr int kStages = COUT <= 64 ? 4 : 3;
+    static constexpr int kTmemCols = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
+    static constexpr int kSmem = kStages * kStage + 1024 + 256;
+};
+
+struct ConvGeom {
+    int N, D, H, W, Wb, R, c0, c1, nseg;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// EPI 0: out bf16 = relu(acc + bias); EPI 1: out fp32 = acc.
+template <int COUT, int EPI>
+__global__ void __launch_bounds__(kCvThreads, 1)
+conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
+                 const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1, const ConvGeom g,
+                 const float *__restrict__ bias, void *__restrict__ out, int *status) {
+    using Cfg = ConvCfg<COUT>;
+    extern __shared__ uint8_t smraw[];
+    const uint32_t raw = smem_addr(smraw);
+    uint8_t *base = smraw + (((raw + 1023u) & ~1023u) - raw);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + Cfg::kStages * Cfg::kStage);
+    uint64_t *empty = full + Cfg::kStages;
+    uint64_t *done = empty + Cfg::kStages;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = g.W / g.Wb, tiles_h = g.H / g.R;
+    int t = blockIdx.x;
+    const int tx = t % tiles_x;
+    t /= tiles_x;
+    const int th = t % tiles_h;
+    t /= tiles_h;
+    const int d = t % g.D, n = t / g.D;
+    const int x0 = tx * g.Wb, h0 = th * g.R;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < Cfg::kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *failed = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, Cfg::kTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int nsteps = 27 * g.nseg;
+
+    if (warp == 0 && lane == 0) {
+        // TMA producer.
+        for (int i = 0; i < nsteps; ++i) {
+            const int s = i % Cfg::kStages;
+            if (i >= Cfg::kStages && !mbar_wait(&empty[s], ((i / Cfg::kStages) - 1) & 1, status)) {
+                *failed = 1;
+                break;
+            }
+            const int tap = i / g.nseg, seg = i - tap * g.nseg;
+            const int c = seg ? g.c1 : g.c0;
+            uint8_t *A = base + s * Cfg::kStage;
+            uint8_t *B = A + Cfg::kABytes;
+            mbar_arrive_expect_tx(&full[s], (uint32_t)((kCvM + COUT) * c * 2));
+            const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+            tma_load_5d(A, seg ? &ta1 : &ta0, 0, x0 + dx, h0 + dy, d + dz, n, &full[s]);
+            tma_load_2d(B, seg ? &tb1 : &tb0, 0, tap * COUT, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer.
+        constexpr uint32_t idesc = umma_idesc_bf16_f32(kCvM, COUT);
+        for (int i = 0; i < nsteps; ++i) {
+            const int s = i % Cfg::kStages;
+            if (!mbar_wait(&full[s], (i / Cfg::kStages) & 1, status)) {
+                *failed = 1;
+                break;
+            }
+            tc_fence_after();
+            const int seg = i % g.nseg;
+            const uint32_t rb = (uint32_t)(seg ? g.c1 : g.c0) * 2u;
+            const uint32_t a_addr = smem_addr(base + s * Cfg::kStage), b_addr = a_addr + Cfg::kABytes;
+            for (uint32_t k = 0; k < rb / 32u; ++k)
+                umma_bf16(tmem, umma_smem_desc(a_addr + 32u * k, rb), umma_smem_desc(b_addr + 32u * k, rb), idesc,
+                          (i > 0 || k > 0) ? 1u : 0u);
+            umma_commit(&empty[s]);
+        }
+        umma_commit(done);
+    }
+    __syncwarp();
+
+    // Epilogue: thread (warp w, lane l) owns tile row 32 w + l.
+    const bool got = mbar_wait(done, 0, status);
+    tc_fence_after();
+    const bool go = __all_sync(0xffffffffu, got && !*failed);
+    if (go) {
+        const int row = warp * 32 + lane;
+        const int hh = h0 + row / g.Wb, xx = x0 + row % g.Wb;
+        const long long vox = (((long long)n * g.D + d) * g.H + hh) * g.W + xx;
+#pragma unroll
+        for (int cb = 0; cb < COUT; cb += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb, v);
+            if (EPI == 0) {
+                uint32_t p[8];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    p[i] = pack_bf16x2(fmaxf(v[2 * i] + bias[cb + 2 * i], 0.0f),
+                                       fmaxf(v[2 * i + 1] + bias[cb + 2 * i + 1], 0.0f));
+                uint4 *o = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + vox * COUT + cb);
+                o[0] = make_uint4(p[0], p[1], p[2], p[3]);
+                o[1] = make_uint4(p[4], p[5], p[6], p[7]);
+            } else {
+                float4 *o = reinterpret_cast<float4 *>(static_cast<float *>(out) + vox * COUT + cb);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, Cfg::kTmemCols);
+    }
+}
+
+// ---- CUDA-core passes -------------------------------------------------------
+
+// x fp32 [N][V] -> bf16 [N][V][16]: channel 0 = x / scale[n], the rest 0.
+__global__ void unet_input_kernel(const float *__restrict__ x, const float *__restrict__ scale,
+                                  __nv_bfloat16 *__restrict__ out, long long vps, long long total) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float v = x[i] / scale[i / vps];
+        uint4 *o = reinterpret_cast<uint4 *>(out + i * 16);
+        o[0] = make_uint4(pack_bf16x2(v, 0.0f), 0u, 0u, 0u);
+        o[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+__device__ __forceinline__ void unpack8(uint4 u, float *f) {
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f[2 * i] = t.x;
+        f[2 * i + 1] = t.y;
+    }
+}
+
+__device__ __forceinline__ uint4 pack8(const float *f) {
+    return make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
+                      pack_bf16x2(f[6], f[7]));
+}
+
+// 2x2x2 average pooling, bf16 [N][D][H][W][C] -> [N][D/2][H/2][W/2][C]; one
+// thread per (output voxel, 8-channel group).
+__global__ void pool2_kernel(const __nv_bfloat16 *__restrict__ in, __nv_bfloat16 *__restrict__ out, int N, int D,
+                             int H, int W, int C) {
+    const int Do = D / 2, Ho = H / 2, Wo = W / 2, G = C / 8;
+    const long long total = (long long)N * Do * Ho * Wo * G;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int gch = (int)(i % G);
+        long long v = i / G;
+        const int x = (int)(v % Wo);
+        v /= Wo;
+        const int y = (int)(v % Ho);
+        v /= Ho;
+        const int z = (int)(v % Do);
+        const int n = (int)(v / Do);
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long src = ((((long long)n * D + 2 * z + (k >> 2)) * H + 2 * y + ((k >> 1) & 1)) * W + 2 * x +
+                                   (k & 1)) * C + gch * 8;
+            float f[8];
+            unpack8(*reinterpret_cast<const uint4 *>(in + src), f);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[j] += f[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[j] *= 0.125f;
+        *reinterpret_cast<uint4 *>(out + i * 8) = pack8(acc);
+    }
+}
+
+// Nearest 2x upsampling, bf16 [N][D/2][H/2][W/2][C] -> [N][D][H][W][C].
+__global__ void up2_kernel(const __nv_bfloat16 *__restrict__ in, __nv_bfloat16 *__restrict__ out, int N, int D,
+                           int H, int W, int C) {
+    const int G = C / 8;
+    const long long total = (long long)N * D * H * W * G;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int gch = (int)(i % G);
+        long long v = i / G;
+        const int x = (int)(v % W);
+        v /= W;
+        const int y = (int)(v % H);
+        v /= H;
+        const int z = (int)(v % D);
+        const int n = (int)(v / D);
+        const long long src = ((((long long)n * (D / 2) + z / 2) * (H / 2) + y / 2) * (W / 2) + x / 2) * C + gch * 8;
+        *reinterpret_cast<uint4 *>(out + i * 8) = *reinterpret_cast<const uint4 *>(in + src);
+    }
+}
+
+// out[v][c] = act[v][c] > 0 ? g[v * gs + go + c] : 0, as bf16 (the gradient
+// through a ReLU whose output is act).
+__global__ void relu_grad_kernel(const float *__restrict__ g, int gs, int go, const __nv_bfloat16 *__restrict__ act,
+                                 __nv_bfloat16 *__restrict__ out, long long nvox, int C) {
+    const long long total = nvox * (C / 8);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long v = i / (C / 8);
+        const int c0 = (int)(i % (C / 8)) * 8;
+        float a[8], r[8];
+        unpack8(*reinterpret_cast<const uint4 *>(act + v * C + c0), a);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = a[j] > 0.0f ? g[v * gs + go + c0 + j] : 0.0f;
+        *reinterpret_cast<uint4 *>(out + v * C + c0) = pack8(r);
+    }
+}
+
+// Gradient through pooling (and the skip branch) and the ReLU before it:
+// out[v][c] = act[v][c] > 0 ? gp[parent(v)][c] / 8 + gskip[v * gs + go + c] : 0.
+__global__ void pool2_grad_kernel(const float *__restrict__ gp, const float *__restrict__ gskip, int gs, int go,
+                                  const __nv_bfloat16 *__restrict__ act, __nv_bfloat16 *__restrict__ out, int N,
+                                  int D, int H, int W, int C) {
+    const int G = C / 8;
+    const long long total = (long long)N * D * H * W * G;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c0 = (int)(i % G) * 8;
+        long long v = i / G;
+        const long long vox = v;
+        const int x = (int)(v % W);
+        v /= W;
+        const int y = (int)(v % H);
+        v /= H;
+        const int z = (int)(v % D);
+        const int n = (int)(v / D);
+        const long long par = (((long long)n * (D / 2) + z / 2) * (H / 2) + y / 2) * (W / 2) + x / 2;
+        float a[8], r[8];
+        unpack8(*reinterpret_cast<const uint4 *>(act + vox * C + c0), a);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            float s = gp[par * C + c0 + j] * 0.125f;
+            if (gskip) s += gskip[vox * gs + go + c0 + j];
+            r[j] = a[j] > 0.0f ? s : 0.0f;
+        }
+        *reinterpret_cast<uint4 *>(out + vox * C + c0) = pack8(r);
+    }
+}
+
+// Gradient through nearest upsampling and the ReLU before it (act at the
+// coarse level): out[p][c] = act[p][c] > 0 ? sum of the 8 children's
+// g[child * gs + go + c] : 0.  D, H, W are the coarse dims.
+__global__ void up2_grad_kernel(const float *__restrict__ g, int gs, int go, const __nv_bfloat16 *__restrict__ act,
+                                __nv_bfloat16 *__restrict__ out, int N, int D, int H, int W, int C) {
+    const int G = C / 8;
+    const long long total = (long long)N * D * H * W * G;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c0 = (int)(i % G) * 8;
+        long long v = i / G;
+        const long long vox = v;
+        const int x = (int)(v % W);
+        v /= W;
+        const int y = (int)(v % H);
+        v /= H;
+        const int z = (int)(v % D);
+        const int n = (int)(v / D);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long ch = ((((long long)n * 2 * D + 2 * z + (k >> 2)) * 2 * H + 2 * y + ((k >> 1) & 1)) * 2 * W +
+                                  2 * x + (k & 1));
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[j] += g[ch * gs + go + c0 + j];
+        }
+        float a[8], r[8];
+        unpack8(*reinterpret_cast<const uint4 *>(act + vox * C + c0), a);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) r[j] = a[j] > 0.0f ? s[j] : 0.0f;
+        *reinterpret_cast<uint4 *>(out + vox * C + c0) = pack8(r);
+    }
+}
+
+// Head: y[v] = x[v] + scale[n] * (sum_c w[c] a[v][c] + b), a bf16 [V][16].
+__global__ void head_kernel(const __nv_bfloat16 *__restrict__ a, const float *__restrict__ wb,
+                            const float *__restrict__ x, const float *__restrict__ scale, float *__restrict__ y,
+                            long long vps, long long total) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        float f[16];
+        unpack8(*reinterpret_cast<const uint4 *>(a + i * 16), f);
+        unpack8(*reinterpret_cast<const uint4 *>(a + i * 16 + 8), f + 8);
+        float s = wb[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) s = fmaf(wb[c], f[c], s);
+        y[i] = x[i] + scale[i / vps] * s;
+    }
+}
+
+// Head gradient: gin = gy * scale (the gradient of the head's sum);
+// ga[v][c] = a[v][c] > 0 ? gin w[c] : 0 (bf16); per-block partial sums of
+// gin a[v][c] (16) and gin (1) -> partials[block][17].
+__global__ void head_grad_kernel(const float *__restrict__ gy, const __nv_bfloat16 *__restrict__ a,
+                                 const float *__restrict__ wb, const float *__restrict__ scale,
+                                 __nv_bfloat16 *__restrict__ ga, float *__restrict__ partials, long long vps,
+                                 long long total) {
+    __shared__ float red[17][256];
+    float acc[17];
+#pragma unroll
+    for (int c = 0; c < 17; ++c) acc[c] = 0.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float gin = gy[i] * scale[i / vps];
+        float f[16], r[16];
+        unpack8(*reinterpret_cast<const uint4 *>(a + i * 16), f);
+        unpack8(*reinterpret_cast<const uint4 *>(a + i * 16 + 8), f + 8);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            acc[c] = fmaf(gin, f[c], acc[c]);
+            r[c] = f[c] > 0.0f ? gin * wb[c] : 0.0f;
+        }
+        acc[16] += gin;
+        *reinterpret_cast<uint4 *>(ga + i * 16) = pack8(r);
+        *reinterpret_cast<uint4 *>(ga + i * 16 + 8) = pack8(r + 8);
+    }
+#pragma unroll
+    for (int c = 0; c < 17; ++c) red[c][threadIdx.x] = acc[c];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int c = 0; c < 17; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 17) partials[blockIdx.x * 17 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// Weight gradient of a 3x3x3 convolution (zero padding):
+//   dW[tap][co][ci] = sum_v g[v][co] * x[v + offset(tap)][ci]
+// Block (chunk, tap): voxels [chunk * kWgChunk, ...) staged 32 at a time in
+// shared memory as fp32; each thread owns (co, ci) pairs tid, tid + 256, ...
+// (at most kWgPairs).  Per-block partials -> partials[chunk][tap][co][ci].
+constexpr int kWgChunk = 8192, kWgVox = 32, kWgPairs = 24;
+
+__global__ void __launch_bounds__(256) wgrad_kernel(const __nv_bfloat16 *__restrict__ x, int cin,
+                                                    const __nv_bfloat16 *__restrict__ g, int cout,
+                                                    float *__restrict__ partials, int N, int D, int H, int W) {
+    extern __shared__ float wsm[];
+    float *gs = wsm;                     // [kWgVox][cout]
+    float *xs = wsm + kWgVox * cout;     // [kWgVox][cin]
+    const int chunk = blockIdx.x, tap = blockIdx.y;
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    const long long V = (long long)N * D * H * W;
+    const long long v0 = (long long)chunk * kWgChunk;
+    const long long v1 = min(V, v0 + kWgChunk);
+    const int npairs = cout * cin;
+    float acc[kWgPairs];
+#pragma unroll
+    for (int k = 0; k < kWgPairs; ++k) acc[k] = 0.0f;
+    for (long long vb = v0; vb < v1; vb += kWgVox) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < kWgVox * cout; e += blockDim.x) {
+            const long long v = vb + e / cout;
+            gs[e] = v < v1 ? __bfloat162float(g[v * cout + e % cout]) : 0.0f;
+        }
+        for (int e = threadIdx.x; e < kWgVox * cin; e += blockDim.x) {
+            const long long v = vb + e / cin;
+            float val = 0.0f;
+            if (v < v1) {
+                long long r = v;
+                const int xx = (int)(r % W) + dx;
+                r /= W;
+                const int yy = (int)(r % H) + dy;
+                r /= H;
+                const int zz = (int)(r % D) + dz;
+                const int n = (int)(r / D);
+                if (xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D)
+                    val = __bfloat162float(x[((((long long)n * D + zz) * H + yy) * W + xx) * cin + e % cin]);
+            }
+            xs[e] = val;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kWgPairs; ++k) {
+            const int p = threadIdx.x + k * 256;
+            if (p < npairs) {
+                const int co = p / cin, ci = p % cin;
+                float s = acc[k];
+                for (int j = 0; j < kWgVox; ++j) s = fmaf(gs[j * cout + co], xs[j * cin + ci], s);
+                acc[k] = s;
+            }
+        }
+    }
+    float *dst = partials + ((long long)chunk * 27 + tap) * npairs;
+#pragma unroll
+    for (int k = 0; k < kWgPairs; ++k) {
+        const int p = threadIdx.x + k * 256;
+        if (p < npairs) dst[p] = acc[k];
+    }
+}
+
+// Bias gradient partials: partials[block][c] = sum over the block's voxels of g[v][c].
+__global__ void colsum_kernel(const __nv_bfloat16 *__restrict__ g, int C, long long nvox,
+                              float *__restrict__ partials) {
+    extern __shared__ float red[];   // [blockDim][C]
+    for (int c = 0; c < C; ++c) red[threadIdx.x * C + c] = 0.0f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox;
+         v += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < C; ++c) red[threadIdx.x * C + c] += __bfloat162float(g[v * C + c]);
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s)
+            for (int c = 0; c < C; ++c) red[threadIdx.x * C + c] += red[(threadIdx.x + s) * C + c];
+        __syncthreads();
+    }
+    if ((int)threadIdx.x < C) partials[blockIdx.x * C + threadIdx.x] = red[threadIdx.x];
+}
+
+static int grid_for(long long n, int threads = 256) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+}
+
+static bool good_c(int c) { return c == 16 || c == 32 || c == 64; }
+
+template <int COUT, int EPI>
+static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0, const CUtensorMap &b1,
+                       const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
+    using Cfg = ConvCfg<COUT>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_kernel<COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             Cfg::kSmem);
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
+        attr = true;
+    }
+    int *status = ctgb_status_ptr();
+    if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
+    const long long tiles = (long long)g.N * g.D * (g.H / g.R) * (g.W / g.Wb);
+    if (tiles > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "conv3d: too many tiles");
+    conv3d_tc_kernel<COUT, EPI><<<(unsigned)tiles, kCvThreads, Cfg::kSmem, st>>>(a0, a1, b0, b1, g, bias, out,
+                                                                                status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d_tc_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+}  // namespace ctgb
+
+using namespace ctgb;
+
+extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int32_t c1, const void *w0,
+                                const void *w1, const float *bias, void *out, int32_t cout, int32_t n, int32_t d,
+                                int32_t h, int32_t w, int32_t mode, void *stream) {
+    clear_error();
+    if (!x0 || !w0 || !out || (c1 && (!x1 || !w1)) || (mode == 0 && !bias))
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: NULL argument");
+    if (!good_c(c0) || !(c1 == 0 || good_c(c1)))
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: input channels must be 16, 32 or 64");
+    if (!(cout == 16 || cout == 32 || cout == 48 || cout == 64 || cout == 96))
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: output channels must be 16, 32, 48, 64 or 96");
+    if (mode != 0 && mode != 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: mode must be 0 or 1");
+    if (n < 1 || d < 1 || h < 1 || w < 16) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: bad volume size");
+    int wb;
+    if (w % 128 == 0) wb = 128;
+    else if (w == 16 || w == 32 || w == 64) wb = w;
+    else return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: W must be 16, 32, 64 or a multiple of 128");
+    const int r = 128 / wb;
+    if (h % r) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: H must be a multiple of %d for W = %d", r, w);
+    ConvGeom g{n, d, h, w, wb, r, c0, c1, c1 ? 2 : 1};
+    CUtensorMap ta0, ta1, tb0, tb1;
+    {
+        const uint64_t dims[5] = {(uint64_t)c0, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
+        const uint32_t box[5] = {(uint32_t)c0, (uint32_t)wb, (uint32_t)r, 1u, 1u};
+        const uint64_t wd[2] = {(uint64_t)c0, (uint64_t)(27 * cout)};
+        const uint32_t wbx[2] = {(uint32_t)c0, (uint32_t)cout};
+        if (!ctgb_make_tmap_bf16(&ta0, x0, 5, dims, box) || !ctgb_make_tmap_bf16(&tb0, w0, 2, wd, wbx))
+            return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: tensor map rejected (alignment?)");
+    }
+    if (c1) {
+        const uint64_t dims[5] = {(uint64_t)c1, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
+        const uint32_t box[5] = {(uint32_t)c1, (uint32_t)wb, (uint32_t)r, 1u, 1u};
+        const uint64_t wd[2] = {(uint64_t)c1, (uint64_t)(27 * cout)};
+        const uint32_t wbx[2] = {(uint32_t)c1, (uint32_t)cout};
+        if (!ctgb_make_tmap_bf16(&ta1, x1, 5, dims, box) || !ctgb_make_tmap_bf16(&tb1, w1, 2, wd, wbx))
+            return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: tensor map rejected (alignment?)");
+    } else {
+        ta1 = ta0;
+        tb1 = tb0;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+#define CTGB_CONV_CASE(CO)                                                                       \
+    case CO:                                                                                    \
+        return mode == 0 ? launch_conv<CO, 0>(ta0, ta1, tb0, tb1, g, bias, out, st)             \
+                         : launch_conv<CO, 1>(ta0, ta1, tb0, tb1, g, bias, out, st);
+    switch (cout) {
+        CTGB_CONV_CASE(16)
+        CTGB_CONV_CASE(32)
+        CTGB_CONV_CASE(48)
+        CTGB_CONV_CASE(64)
+        CTGB_CONV_CASE(96)
+    }
+#undef CTGB_CONV_CASE
+    return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: unsupported output channels");
+}
+
+static int ew_done(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_unet_input(const float *x, const float *scale, void *out, int32_t n, int64_t vps, void *stream) {
+    clear_error();
+    if (!x || !scale || !out || n < 1 || vps < 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_input: bad arguments");
+    const long long total = (long long)n * vps;
+    unet_input_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        x, scale, static_cast<__nv_bfloat16 *>(out), vps, total);
+    return ew_done("unet_input_kernel");
+}
+
+extern "C" int ctgb_unet_pool2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c,
+                               void *stream) {
+    clear_error();
+    if (!in || !out || c % 8 || c < 8 || d % 2 || h % 2 || w % 2 || n < 1 || d < 2)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_pool2: bad arguments");
+    const long long total = (long long)n * (d / 2) * (h / 2) * (w / 2) * (c / 8);
+    pool2_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(in), static_cast<__nv_bfloat16 *>(out), n, d, h, w, c);
+    return ew_done("pool2_kernel");
+}
+
+extern "C" int ctgb_unet_up2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c,
+                             void *stream) {
+    clear_error();
+    if (!in || !out || c % 8 || c < 8 || d % 2 || h % 2 || w % 2 || n < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_up2: bad arguments");
+    const long long total = (long long)n * d * h * w * (c / 8);
+    up2_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(in), static_cast<__nv_bfloat16 *>(out), n, d, h, w, c);
+    return ew_done("up2_kernel");
+}
+
+extern "C" int ctgb_unet_relu_grad(const float *g, int32_t gs, int32_t go, const void *act, void *out, int64_t nvox,
+                                   int32_t c, void *stream) {
+    clear_error();
+    if (!g || !act || !out || c % 8 || c < 8 || go < 0 || go + c > gs || nvox < 0)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_relu_grad: bad arguments");
+    relu_grad_kernel<<<grid_for(nvox * (c / 8)), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        g, gs, go, static_cast<const __nv_bfloat16 *>(act), static_cast<__nv_bfloat16 *>(out), nvox, c);
+    return ew_done("relu_grad_kernel");
+}
+
+extern "C" int ctgb_unet_pool2_grad(const float *gp, const float *gskip, int32_t gs, int32_t go, const void *act,
+                                    void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void *stream) {
+    clear_error();
+    if (!gp || !act || !out || c % 8 || c < 8 || d % 2 || h % 2 || w % 2 || (gskip && (go < 0 || go + c > gs)))
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_pool2_grad: bad arguments");
+    const long long total = (long long)n * d * h * w * (c / 8);
+    pool2_grad_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        gp, gskip, gs, go, static_cast<const __nv_bfloat16 *>(act), static_cast<__nv_bfloat16 *>(out), n, d, h, w,
+        c);
+    return ew_done("pool2_grad_kernel");
+}
+
+extern "C" int ctgb_unet_up2_grad(const float *g, int32_t gs, int32_t go, const void *act, void *out, int32_t n,
+                                  int32_t d, int32_t h, int32_t w, int32_t c, void *stream) {
+    clear_error();
+    if (!g || !act || !out || c % 8 || c < 8 || go < 0 || go + c > gs)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_up2_grad: bad arguments");
+    const long long total = (long long)n * d * h * w * (c / 8);
+    up2_grad_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        g, gs, go, static_cast<const __nv_bfloat16 *>(act), static_cast<__nv_bfloat16 *>(out), n, d, h, w, c);
+    return ew_done("up2_grad_kernel");
+}
+
+extern "C" int ctgb_unet_head(const void *a, const float *wb, const float *x, const float *scale, float *y, int32_t n,
+                              int64_t vps, void *stream) {
+    clear_error();
+    if (!a || !wb || !x || !scale || !y || n < 1 || vps < 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_head: bad arguments");
+    const long long total = (long long)n * vps;
+    head_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(a), wb, x, scale, y, vps, total);
+    return ew_done("head_kernel");
+}
+
+extern "C" int ctgb_unet_head_grad_blocks(int64_t total, int32_t *blocks) {
+    clear_error();
+    if (!blocks || total < 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_head_grad_blocks: bad arguments");
+    *blocks = grid_for(total);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_unet_head_grad(const float *gy, const void *a, const float *wb, const float *scale, void *ga,
+                                   float *partials, int32_t n, int64_t vps, void *stream) {
+    clear_error();
+    if (!gy || !a || !wb || !scale || !ga || !partials || n < 1 || vps < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_head_grad: bad arguments");
+    const long long total = (long long)n * vps;
+    head_grad_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        gy, static_cast<const __nv_bfloat16 *>(a), wb, scale, static_cast<__nv_bfloat16 *>(ga), partials, vps,
+        total);
+    return ew_done("head_grad_kernel");
+}
+
+extern "C" int ctgb_unet_wgrad_chunks(int32_t n, int32_t d, int32_t h, int32_t w, int32_t *chunks) {
+    clear_error();
+    if (!chunks || n < 1 || d < 1 || h < 1 || w < 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad_chunks: bad arguments");
+    const long long V = (long long)n * d * h * w;
+    *chunks = (int)((V + kWgChunk - 1) / kWgChunk);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, float *partials, int32_t n,
+                               int32_t d, int32_t h, int32_t w, void *stream) {
+    clear_error();
+    if (!x || !g || !partials || cin < 1 || cout < 1 || cin * cout > 256 * kWgPairs || n < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: bad arguments");
+    const long long V = (long long)n * d * h * w;
+    const int chunks = (int)((V + kWgChunk - 1) / kWgChunk);
+    const size_t smem = sizeof(float) * kWgVox * (size_t)(cin + cout);
+    dim3 grid(chunks, 27);
+    wgrad_kernel<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(x), cin, static_cast<const __nv_bfloat16 *>(g), cout, partials, n, d, h,
+        w);
+    return ew_done("wgrad_kernel");
+}
+
+extern "C" int ctgb_unet_colsum(const void *g, int32_t c, int64_t nvox, float *partials, int32_t blocks,
+                                void *stream) {
+    clear_error();
+    if (!g || !partials || c < 1 || c > 64 || nvox < 1 || blocks < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_colsum: bad arguments");
+    const int threads = 128;
+    colsum_kernel<<<blocks, threads, sizeof(float) * threads * c, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(g), c, nvox, partials);
+    return ew_done("colsum_kernel");
+}

@@ -262,9 +262,19 @@ def tv_descent(x, step, ng, eps=1e-7):
 
 
 def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.007, r_max=0.99, alpha_red=0.95,
-             eps=1e-7, x0=None, phantom=None, matched=False, norms=None, filter_type=None, cutoff=None):
+             eps=1e-7, x0=None, phantom=None, matched=False, norms=None, filter_type=None, cutoff=None, prox=None,
+             on_tv=None, times=None):
     """ASD_POCS.py:137-201.  x0 defaults to the script's FBP start
-    (Filtering() then backward() of proj0).  Returns (x, rmse list, log)."""
+    (Filtering() then backward() of proj0).  Returns (x, rmse list, log).
+
+    prox: optional replacement of the TV-descent step (ASD_POCS.py:186-190):
+    called as prox(x, plain) where plain() runs the script's ng TV steps on
+    a copy and returns it; prox returns the new volume (it may return
+    plain(), e.g. as a fallback).  on_tv(pre, post): called with the volume
+    before and after each TV step (training pairs for a learned prox).
+    times: optional list that receives the wall time (s, device-synchronised)
+    at the end of every iteration."""
+    import time as _time
     P = P if isinstance(P, Projector) else Projector(P)
     dev = P.device
     S = _Scratch(P, dev)
@@ -281,6 +291,7 @@ def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.
     n_p, n_v = _n(S.proj), _n(x)
     rmse, log = [], []
     nz, ny, nx = x.shape
+    t0 = _time.perf_counter()
     for _ in range(niter):
         f0.copy_(x)
         for _a in range(na):
@@ -292,12 +303,20 @@ def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.
         dp = math.sqrt(_sqdist(S, x, f0).item())
         dtvg = alpha * dp
         f0.copy_(x)
-        a, b = x, tv_a
-        for _g in range(ng):
-            _lib.call("ctgb_tv_step", _ptr(a), _ptr(b), nz, ny, nx, eps, float(dtvg), _ptr(S.partials), _stream())
-            a, b = b, (tv_b if b is tv_a else tv_a)
-        if a is not x:
-            x.copy_(a)
+
+        def plain(src=x, step=dtvg):
+            a, b = src, tv_a
+            for _g in range(ng):
+                _lib.call("ctgb_tv_step", _ptr(a), _ptr(b), nz, ny, nx, eps, float(step), _ptr(S.partials),
+                          _stream())
+                a, b = b, (tv_b if b is tv_a else tv_a)
+            return a
+
+        new = plain() if prox is None else prox(x, plain)
+        if on_tv is not None:
+            on_tv(f0, new)
+        if new is not x:
+            x.copy_(new)
         dg = math.sqrt(_sqdist(S, x, f0).item())
         if dg > r_max * dp:
             alpha *= alpha_red
@@ -305,6 +324,9 @@ def asd_pocs(P, proj0, niter=20, beta=1.0, beta_red=0.999, na=5, ng=20, alpha=0.
         log.append({"dtvg": dtvg, "beta": beta, "dp": dp, "dg": dg, "alpha": alpha})
         if phantom is not None:
             rmse.append(_rmse(S, x, phantom))
+        if times is not None:
+            torch.cuda.synchronize(dev)
+            times.append(_time.perf_counter() - t0)
     return x, rmse, log
 
 

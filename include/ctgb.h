@@ -252,6 +252,58 @@ int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, int32_t n2, f
                  double *partials, void *stream);
 int ctgb_sqdist(const float *a, const float *b, int64_t n, double *partials, double *out, void *stream);
 
+/* ---- learned proximal step: 3-D U-Net blocks ---------------------------------
+ * No reference counterpart (the network stands in for ASD-POCS's TV descent,
+ * python/ASD_POCS.py:186-190).  Activations bf16 [N][D][H][W][C] (channels
+ * innermost), conv weights bf16 [27 taps][Cout][Cin] with tap =
+ * (dz+1)*9 + (dy+1)*3 + (dx+1), fp32 accumulation.
+ *
+ * ctgb_unet_conv3d: 3x3x3 convolution, zero padding, on the tcgen05 tensor
+ * cores.  Input = channel concat of x0 (c0 channels) and, when c1 > 0, x1
+ * (c1 channels), c0, c1 in {16, 32, 64}; w0 / w1 are the weight blocks of
+ * the two segments ([27][cout][c0], [27][cout][c1]); cout in {16, 32, 48,
+ * 64, 96}.  mode 0: out bf16 = relu(conv + bias); mode 1: out fp32 = conv
+ * (bias unused).  W must be 16, 32, 64 or a multiple of 128, and H a
+ * multiple of 128 / min(W, 128). */
+int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int32_t c1, const void *w0, const void *w1,
+                     const float *bias, void *out, int32_t cout, int32_t n, int32_t d, int32_t h, int32_t w,
+                     int32_t mode, void *stream);
+/* x fp32 [n][vps] -> bf16 [n][vps][16] with channel 0 = x / scale[sample]. */
+int ctgb_unet_input(const float *x, const float *scale, void *out, int32_t n, int64_t vps, void *stream);
+/* 2x2x2 average pooling and nearest 2x upsampling (bf16, c a multiple of 8;
+ * d, h, w are the fine dims for pooling and the output dims for upsampling). */
+int ctgb_unet_pool2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void *stream);
+int ctgb_unet_up2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void *stream);
+/* Gradients through a ReLU whose output is act (bf16 [nvox][c]), reading
+ * channels go .. go+c-1 of a gradient with gs channels per voxel:
+ * relu_grad (same level), pool2_grad (gp at the coarse level / 8, plus an
+ * optional skip gradient; d, h, w fine dims), up2_grad (sum of the 8 fine
+ * children; d, h, w coarse dims).  Outputs bf16 [.][c]. */
+int ctgb_unet_relu_grad(const float *g, int32_t gs, int32_t go, const void *act, void *out, int64_t nvox, int32_t c,
+                        void *stream);
+int ctgb_unet_pool2_grad(const float *gp, const float *gskip, int32_t gs, int32_t go, const void *act, void *out,
+                         int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void *stream);
+int ctgb_unet_up2_grad(const float *g, int32_t gs, int32_t go, const void *act, void *out, int32_t n, int32_t d,
+                       int32_t h, int32_t w, int32_t c, void *stream);
+/* 1x1x1 head with residual: y = x + scale[sample] * (sum_c wb[c] a[c] + wb[16]).
+ * head_grad: ga = relu'(a) * gy * scale * wb[c] (bf16) and per-block partial
+ * sums [blocks][17] of (gy * scale * a[c], gy * scale); blocks from
+ * ctgb_unet_head_grad_blocks. */
+int ctgb_unet_head(const void *a, const float *wb, const float *x, const float *scale, float *y, int32_t n,
+                   int64_t vps, void *stream);
+int ctgb_unet_head_grad_blocks(int64_t total, int32_t *blocks);
+int ctgb_unet_head_grad(const float *gy, const void *a, const float *wb, const float *scale, void *ga,
+                        float *partials, int32_t n, int64_t vps, void *stream);
+/* Weight gradient of one input segment: partials[chunk][27][cout][cin] of
+ * sum_v g[v][co] x[v + tap][ci] (chunks from ctgb_unet_wgrad_chunks; the
+ * caller sums over chunks).  cin * cout <= 6144. */
+int ctgb_unet_wgrad_chunks(int32_t n, int32_t d, int32_t h, int32_t w, int32_t *chunks);
+int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, float *partials, int32_t n, int32_t d,
+                    int32_t h, int32_t w, void *stream);
+/* Per-block channel sums of a bf16 [nvox][c] gradient (c <= 64) ->
+ * partials[blocks][c] (the bias gradient after a sum over blocks). */
+int ctgb_unet_colsum(const void *g, int32_t c, int64_t nvox, float *partials, int32_t blocks, void *stream);
+
 /* ---- status ----------------------------------------------------------------
  * ctgb_device_status: the device-side status word of the current device
  * (CTGB_DEVERR_* bits set by kernels whose bounded waits ran out).  Reads it
