@@ -231,7 +231,10 @@ bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj,
 // source height the v footprint ends move linearly with z, so they are one
 // FMA each.  Running sums are accumulated in double and stored rounded, so
 // each lookup carries one float32 rounding of the prefix, not a drifting sum.
-constexpr int kBiZ = 16;
+#ifndef CTGB_BI_Z
+#define CTGB_BI_Z 16
+#endif
+constexpr int kBiZ = CTGB_BI_Z;   // z voxels per thread
 #ifndef CTGB_BI_BLOCKS
 #define CTGB_BI_BLOCKS 6
 #endif

@@ -105,6 +105,30 @@ class Projector:
                       view0, nviews, sc, int(bool(accumulate)), _ptr(ws), ws.numel() * 4, _stream())
         return out
 
+    def ray_forward(self, vol, out=None, view0=0, nviews=None):
+        """Siddon ray sums to every pixel centre (the `Method: 'Ray'` projector)."""
+        view0, nviews = self._views(view0, nviews)
+        self._check(vol, self.volume_shape, "vol")
+        if out is None:
+            out = torch.empty(self.proj_shape(nviews), dtype=torch.float32, device=vol.device)
+        self._check(out, self.proj_shape(nviews), "out")
+        _lib.call("ctgb_ray_forward", ctypes.byref(self.c), _ptr(self.table), _ptr(vol), _ptr(out), view0, nviews,
+                  _stream())
+        return out
+
+    def ray_backproject(self, proj, out=None, view0=0, nviews=None, scale=1.0, accumulate=False):
+        """vol = scale * transpose of ray_forward (exact adjoint up to float
+        rounding; atomics make the summation order run-dependent)."""
+        view0, nviews = self._views(view0, nviews)
+        self._check(proj, self.proj_shape(nviews), "proj")
+        if out is None:
+            out = torch.empty(self.volume_shape, dtype=torch.float32, device=proj.device)
+            accumulate = False
+        self._check(out, self.volume_shape, "out")
+        _lib.call("ctgb_ray_backproject", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out), view0,
+                  nviews, float(scale), int(bool(accumulate)), _stream())
+        return out
+
     def forward_launches(self, view0=0, nviews=None):
         """Kernel launches one forward() call makes over this view range."""
         view0, nviews = self._views(view0, nviews)

@@ -91,22 +91,29 @@ class Reconstruction:
 
     # -- projectors ----------------------------------------------------------------
     def forward(self):
-        """self.proj = DD forward projection of self.image (distance_forward)."""
-        if self.Method != 'Distance':
+        """self.proj = forward projection of self.image: DD (distance_forward)
+        for Method 'Distance', Siddon ray sums for Method 'Ray' (a stub in
+        the reference, Reconstruction_numba.py:799-801)."""
+        if self.Method not in ('Distance', 'Ray'):
             return
         host = not isinstance(self.image, torch.Tensor)
         vol = _to_device(self.image, self.projector.device)
-        proj = self.projector.forward(vol)
+        proj = self.projector.forward(vol) if self.Method == 'Distance' else self.projector.ray_forward(vol)
         self.proj = _host(proj) if host else proj
 
     def backward(self):
         """self.image = FDK-weighted DD backprojection of self.proj * dtheta
-        (distance_backproj)."""
-        if self.Method != 'Distance':
+        (distance_backproj) for Method 'Distance'; for Method 'Ray' (a stub
+        in the reference, :266-268) the transpose of the ray projector times
+        dtheta."""
+        if self.Method not in ('Distance', 'Ray'):
             return
         host = not isinstance(self.proj, torch.Tensor)
         q = _to_device(self.proj, self.projector.device)
-        vol = self.projector.backproject_fdk(q)
+        if self.Method == 'Distance':
+            vol = self.projector.backproject_fdk(q)
+        else:
+            vol = self.projector.ray_backproject(q, scale=self.projector.params.dtheta)
         self.image = _host(vol) if host else vol
 
     def Filtering(self):

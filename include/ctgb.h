@@ -252,6 +252,17 @@ int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, int32_t n2, f
                  double *partials, void *stream);
 int ctgb_sqdist(const float *a, const float *b, int64_t n, double *partials, double *out, void *stream);
 
+/* ---- ray-driven (Siddon) projection -----------------------------------------
+ * The `Method: 'Ray'` projector (Reconstruction_numba.py:788-789 and
+ * :266-268, stubs there; algorithm of matlab/RayDrivenProjection3DSiddon.m
+ * :55-180): proj = line integrals of vol along the rays from the source to
+ * every pixel centre (same geometry table as ctgb_forward);
+ * ctgb_ray_backproject: vol = (accumulate ? vol : 0) + scale * transpose. */
+int ctgb_ray_forward(const ctgb_params *p, const void *d_table, const float *d_vol, float *d_proj, int32_t view0,
+                     int32_t nviews, void *stream);
+int ctgb_ray_backproject(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol, int32_t view0,
+                         int32_t nviews, float scale, int32_t accumulate, void *stream);
+
 /* ---- learned proximal step: 3-D U-Net blocks ---------------------------------
  * No reference counterpart (the network stands in for ASD-POCS's TV descent,
  * python/ASD_POCS.py:186-190).  Activations bf16 [N][D][H][W][C] (channels

@@ -301,3 +301,127 @@ void ct_backproject_fdk(const ct_geom *g, const double *angles, int view0, int n
     }
     free(ki); free(pp);
 }
+
+/* ---- ray-driven (Siddon) projection -----------------------------------------
+ * matlab/RayDrivenProjection3DSiddon.m:55-180 restated on the Python class's
+ * geometry (the `Method: 'Ray'` branch of distance_forward,
+ * python/Reconstruction_numba.py:788-789, traces from the source to each
+ * detector pixel centre through the same voxel planes): parametric plane
+ * crossings alpha = (plane - S) / (P - S) per axis, the entry/exit
+ * [alpha_min, alpha_max] clipped to [0, 1], the crossings inside merged and
+ * de-duplicated within 1e-6 (uniquetol), each segment's length
+ * |P - S| * (alpha_{i+1} - alpha_i) times the voxel holding its midpoint. */
+static int cmp_double(const void *a, const void *b) {
+    double x = *(const double *)a, y = *(const double *)b;
+    return (x > y) - (x < y);
+}
+
+typedef void (*ray_visit_fn)(void *ctx, long vox, double len);
+
+static void siddon_ray(const ct_geom *g, const double S[3], const double P[3], const double *const plane[3],
+                       const double d[3], const int n[3], double *buf, ray_visit_fn visit, void *ctx) {
+    const double tol_min = 1e-6;
+    double amin = 0.0, amax = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        double den = P[a] - S[a];
+        if (fabs(den) < tol_min) {
+            /* parallel to the planes of this axis: inside or not at all */
+            double lo = plane[a][0] < plane[a][n[a]] ? plane[a][0] : plane[a][n[a]];
+            double hi = plane[a][0] < plane[a][n[a]] ? plane[a][n[a]] : plane[a][0];
+            if (S[a] < lo || S[a] > hi) return;
+            continue;
+        }
+        double a0 = (plane[a][0] - S[a]) / den, a1 = (plane[a][n[a]] - S[a]) / den;
+        double lo = a0 < a1 ? a0 : a1, hi = a0 < a1 ? a1 : a0;
+        if (lo > amin) amin = lo;
+        if (hi < amax) amax = hi;
+    }
+    if (amin > amax || fabs(amin - amax) < tol_min) return;
+    int m = 0;
+    buf[m++] = amin;
+    for (int a = 0; a < 3; ++a) {
+        double den = P[a] - S[a];
+        if (fabs(den) < tol_min) continue;
+        for (int i = 0; i <= n[a]; ++i) {
+            double al = (plane[a][i] - S[a]) / den;
+            if (al > amin && al < amax) buf[m++] = al;
+        }
+    }
+    buf[m++] = amax;
+    qsort(buf, (size_t)m, sizeof(double), cmp_double);
+    int k = 1;
+    for (int i = 1; i < m; ++i)
+        if (buf[i] - buf[k - 1] > tol_min) buf[k++] = buf[i];
+    double d12 = sqrt((S[0] - P[0]) * (S[0] - P[0]) + (S[1] - P[1]) * (S[1] - P[1]) + (S[2] - P[2]) * (S[2] - P[2]));
+    for (int i = 0; i + 1 < k; ++i) {
+        double am = 0.5 * (buf[i] + buf[i + 1]);
+        int idx[3];
+        int ok = 1;
+        for (int a = 0; a < 3; ++a) {
+            double f = (S[a] + am * (P[a] - S[a]) - plane[a][0]) / d[a];
+            if (fabs(f) <= tol_min) f = 0.0;
+            idx[a] = (int)floor(f);
+            if (idx[a] < 0 || idx[a] >= n[a]) ok = 0;
+        }
+        if (!ok) continue;
+        visit(ctx, ((long)idx[2] * g->ny + idx[1]) * g->nx + idx[0], d12 * (buf[i + 1] - buf[i]));
+    }
+}
+
+static void ray_planes(const ct_geom *g, double **xp, double **yp, double **zp, double d[3]) {
+    *xp = malloc(sizeof(double) * (g->nx + 1));
+    *yp = malloc(sizeof(double) * (g->ny + 1));
+    *zp = malloc(sizeof(double) * (g->nz + 1));
+    make_planes(g, *xp, *yp, *zp, d);
+}
+
+/* proj[(view-view0)][nv][nu] = ray sums of vol. */
+void ct_ray_forward(const ct_geom *g, const double *angles, int view0, int nview, const float *vol, double *proj,
+                    int nthreads) {
+    double *xp, *yp, *zp, d[3];
+    ray_planes(g, &xp, &yp, &zp, d);
+    const double *plane[3] = {xp, yp, zp};
+    const int n[3] = {g->nx, g->ny, g->nz};
+    const long npix = (long)g->nu * g->nv;
+    const int cap = g->nx + g->ny + g->nz + 8;
+#pragma omp parallel num_threads(nthreads)
+    {
+        double *buf = malloc(sizeof(double) * cap);
+#pragma omp for schedule(dynamic, 64)
+        for (long t = 0; t < (long)nview * npix; ++t) {
+            int v = (int)(t / npix) + view0;
+            int r = (int)((t % npix) / g->nu), c = (int)(t % g->nu);
+            double S[3], D[3], P[3];
+            view_positions(g, angles[v], S, D);
+            det_point(g, S, angles[v], u_center(g, c), v_center(g, r), P);
+            gather_ctx ctx = {vol, 0.0};
+            siddon_ray(g, S, P, plane, d, n, buf, gather_visit, &ctx);
+            proj[t] = ctx.acc;
+        }
+        free(buf);
+    }
+    free(xp); free(yp); free(zp);
+}
+
+/* vol += transpose of ct_ray_forward applied to proj (serial). */
+void ct_ray_backproject(const ct_geom *g, const double *angles, int view0, int nview, const float *proj,
+                        double *vol) {
+    double *xp, *yp, *zp, d[3];
+    ray_planes(g, &xp, &yp, &zp, d);
+    const double *plane[3] = {xp, yp, zp};
+    const int n[3] = {g->nx, g->ny, g->nz};
+    const long npix = (long)g->nu * g->nv;
+    double *buf = malloc(sizeof(double) * (g->nx + g->ny + g->nz + 8));
+    for (int v = view0; v < view0 + nview; ++v) {
+        double S[3], D[3], P[3];
+        view_positions(g, angles[v], S, D);
+        for (long p = 0; p < npix; ++p) {
+            scatter_ctx ctx = {vol, (double)proj[(long)(v - view0) * npix + p]};
+            if (ctx.val == 0.0) continue;
+            det_point(g, S, angles[v], u_center(g, (int)(p % g->nu)), v_center(g, (int)(p / g->nu)), P);
+            siddon_ray(g, S, P, plane, d, n, buf, scatter_visit, &ctx);
+        }
+    }
+    free(buf);
+    free(xp); free(yp); free(zp);
+}

@@ -54,6 +54,10 @@ def lib():
                                                 P(ctypes.c_float), P(ctypes.c_double)]
         _LIB.ct_backproject_fdk.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, P(ctypes.c_float), P(ctypes.c_double), ctypes.c_int]
+        _LIB.ct_ray_forward.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
+                                        P(ctypes.c_float), P(ctypes.c_double), ctypes.c_int]
+        _LIB.ct_ray_backproject.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
+                                            P(ctypes.c_float), P(ctypes.c_double)]
     return _LIB
 
 
@@ -135,6 +139,23 @@ class OracleGeometry:
         q = np.ascontiguousarray(proj, dtype=np.float32).reshape(nview, self.nv, self.nu)
         out = np.zeros((self.nz, self.ny, self.nx), dtype=np.float64)
         lib().ct_backproject_matched(ctypes.byref(self.g), _dp(self.angles), view0, nview, _fp(q), _dp(out))
+        return out
+
+    def ray_forward(self, image, view0=0, nview=None, nthreads=0):
+        """Siddon ray sums (matlab/RayDrivenProjection3DSiddon.m) to every pixel centre."""
+        nview = self.nviews - view0 if nview is None else nview
+        vol = np.ascontiguousarray(image, dtype=np.float32).reshape(self.nz, self.ny, self.nx)
+        out = np.zeros((nview, self.nv, self.nu), dtype=np.float64)
+        lib().ct_ray_forward(ctypes.byref(self.g), _dp(self.angles), view0, nview, _fp(vol), _dp(out),
+                             nthreads or os.cpu_count())
+        return out
+
+    def ray_backward(self, proj, view0=0, nview=None):
+        """Transpose of ray_forward."""
+        nview = self.nviews - view0 if nview is None else nview
+        q = np.ascontiguousarray(proj, dtype=np.float32).reshape(nview, self.nv, self.nu)
+        out = np.zeros((self.nz, self.ny, self.nx), dtype=np.float64)
+        lib().ct_ray_backproject(ctypes.byref(self.g), _dp(self.angles), view0, nview, _fp(q), _dp(out))
         return out
 
     # -- FDK filtering (Reconstruction_numba.py:190-259) ----------------------
