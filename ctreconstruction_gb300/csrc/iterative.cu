@@ -104,11 +104,12 @@ __device__ __forceinline__ float tv_term(const float *__restrict__ x, int n1, in
     return t1 + t2 + t3 + t4;
 }
 
-// Pass 1: per-block partial sums of dtv^2 over the interior.  Each warp
-// walks whole rows (i, j) of the array (rows distributed grid-stride over the
-// block's warps), its lanes striding along k, so the only integer division
-// is one 32-bit split of the row index per row.
-__global__ void tv_norm_kernel(const float *__restrict__ x, int n0, int n1, int n2, float eps,
+// Pass 1: dtv at every interior voxel, written to y (the output array, used
+// as scratch), and per-block partial sums of dtv^2.  Each warp walks whole
+// rows (i, j) of the array (rows distributed grid-stride over the block's
+// warps), its lanes striding along k, so the only integer division is one
+// 32-bit split of the row index per row.
+__global__ void tv_norm_kernel(const float *__restrict__ x, float *__restrict__ y, int n0, int n1, int n2, float eps,
                                double *__restrict__ partials) {
     __shared__ double red[kEwThreads / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -116,9 +117,11 @@ __global__ void tv_norm_kernel(const float *__restrict__ x, int n0, int n1, int 
     double acc = 0.0;
     for (unsigned r = blockIdx.x * wpb + warp; r < rows; r += gridDim.x * wpb) {
         const int i = (int)(r / m1) + 1, j = (int)(r % m1) + 1;
+        float *__restrict__ yrow = y + ((long long)i * n1 + j) * n2;
         float racc = 0.0f;
         for (int k = 1 + lane; k < n2 - 1; k += 32) {
             const float d = tv_term(x, n1, n2, i, j, k, eps);
+            yrow[k] = d;
             racc = fmaf(d, d, racc);
         }
         acc += (double)racc;
@@ -150,9 +153,9 @@ __global__ void __launch_bounds__(kReduceThreads) reduce_partials_kernel(double 
     if (threadIdx.x == 0) partials[0] = red[0];
 }
 
-// Pass 2: y = x - step * dtv / ||dtv|| (||dtv|| -> 1 when below eps), with
-// ||dtv||^2 in partials[0]; the border of y is x's border (tv_grad pads dtv
-// with zeros).  Rows as in pass 1.
+// Pass 2 (streaming): y = x - step * dtv / ||dtv|| with dtv from pass 1 in y
+// (||dtv|| -> 1 when below eps) and ||dtv||^2 in partials[0]; the border of y
+// is x's border (tv_grad pads dtv with zeros).
 __global__ void tv_step_kernel(const float *__restrict__ x, float *__restrict__ y, int n0, int n1, int n2, float eps,
                                const double *__restrict__ partials, float step) {
     float nrm = (float)sqrt(partials[0]);
@@ -166,7 +169,7 @@ __global__ void tv_step_kernel(const float *__restrict__ x, float *__restrict__ 
         const bool inner_row = i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
         for (int k = lane; k < n2; k += 32) {
             float v = x[base + k];
-            if (inner_row && k > 0 && k < n2 - 1) v = v - step * (tv_term(x, n1, n2, i, j, k, eps) * inv);
+            if (inner_row && k > 0 && k < n2 - 1) v = v - step * (y[base + k] * inv);
             y[base + k] = v;
         }
     }
@@ -300,7 +303,7 @@ extern "C" int ctgb_tv_step(const float *x, float *y, int32_t n0, int32_t n1, in
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "ctgb_tv_step: %s", cudaGetErrorString(e));
         return CTGB_OK;
     }
-    tv_norm_kernel<<<nb, kEwThreads, 0, st>>>(x, n0, n1, n2, eps, partials);
+    tv_norm_kernel<<<nb, kEwThreads, 0, st>>>(x, y, n0, n1, n2, eps, partials);
     reduce_partials_kernel<<<1, kReduceThreads, 0, st>>>(partials, nb);
     tv_step_kernel<<<nb, kEwThreads, 0, st>>>(x, y, n0, n1, n2, eps, partials, step);
     return launched("ctgb_tv_step");

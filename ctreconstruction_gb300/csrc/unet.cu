@@ -11,8 +11,8 @@
 // loop runs over the 27 taps (x the input segments of a channel concat):
 // per step TMA brings the 128 shifted input voxels (a box {C, Wb, R, 1, 1} of
 // the 5-D activation tensor; zero fill outside the volume is the conv's zero
-// padding) and the tap's [Cout][C] weight block into a 4-stage ring of
-// shared-memory buffers, in the swizzled K-major layout tcgen05 reads; one
+// padding) and the tap's [Cout][C] weight block into a ring of 3-8
+// shared-memory stages (sized for the layer's widest segment), in the swizzled K-major layout tcgen05 reads; one
 // thread issues tcgen05.mma (M = 128, N = Cout, K = 16 per instruction)
 // into a TMEM accumulator, and tcgen05.commit releases each stage.  The
 // epilogue reads TMEM with tcgen05.ld (one row per thread), adds the bias,
@@ -34,12 +34,14 @@ namespace ctgb {
 
 constexpr int kCvM = 128, kCvThreads = 128;
 
-template <int COUT>
+// Stage buffers sized for the widest input segment (CMAX channels), so that
+// narrow layers keep more stages (and more CTAs per SM) in flight.
+template <int COUT, int CMAX>
 struct ConvCfg {
-    static constexpr int kABytes = kCvM * 128;                          // 128 rows of up to 128 B
-    static constexpr int kBBytes = ((COUT * 128 + 1023) / 1024) * 1024;  // COUT rows of up to 128 B
+    static constexpr int kABytes = kCvM * CMAX * 2;                          // 128 rows of CMAX bf16
+    static constexpr int kBBytes = ((COUT * CMAX * 2 + 1023) / 1024) * 1024;  // COUT rows of CMAX bf16
     static constexpr int kStage = kABytes + kBBytes;
-    static constexpr int kStages = COUT <= 64 ? 4 : 3;
+    static constexpr int kStages = (65536 / kStage) < 3 ? 3 : ((65536 / kStage) > 8 ? 8 : 65536 / kStage);
     static constexpr int kTmemCols = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
     static constexpr int kSmem = kStages * kStage + 1024 + 256;
 };
@@ -54,12 +56,12 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
 }
 
 // EPI 0: out bf16 = relu(acc + bias); EPI 1: out fp32 = acc.
-template <int COUT, int EPI>
+template <int COUT, int CMAX, int EPI>
 __global__ void __launch_bounds__(kCvThreads, 1)
 conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                  const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1, const ConvGeom g,
                  const float *__restrict__ bias, void *__restrict__ out, int *status) {
-    using Cfg = ConvCfg<COUT>;
+    using Cfg = ConvCfg<COUT, CMAX>;
     extern __shared__ uint8_t smraw[];
     const uint32_t raw = smem_addr(smraw);
     uint8_t *base = smraw + (((raw + 1023u) & ~1023u) - raw);
@@ -476,14 +478,14 @@ static int grid_for(long long n, int threads = 256) {
 
 static bool good_c(int c) { return c == 16 || c == 32 || c == 64; }
 
-template <int COUT, int EPI>
+template <int COUT, int CMAX, int EPI>
 static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0, const CUtensorMap &b1,
                        const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
-    using Cfg = ConvCfg<COUT>;
+    using Cfg = ConvCfg<COUT, CMAX>;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_kernel<COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             Cfg::kSmem);
+        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_kernel<COUT, CMAX, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
         attr = true;
     }
@@ -491,8 +493,8 @@ static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUten
     if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
     const long long tiles = (long long)g.N * g.D * (g.H / g.R) * (g.W / g.Wb);
     if (tiles > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "conv3d: too many tiles");
-    conv3d_tc_kernel<COUT, EPI><<<(unsigned)tiles, kCvThreads, Cfg::kSmem, st>>>(a0, a1, b0, b1, g, bias, out,
-                                                                                status);
+    conv3d_tc_kernel<COUT, CMAX, EPI><<<(unsigned)tiles, kCvThreads, Cfg::kSmem, st>>>(a0, a1, b0, b1, g, bias,
+                                                                                      out, status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d_tc_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
@@ -542,10 +544,17 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
         tb1 = tb0;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-#define CTGB_CONV_CASE(CO)                                                                       \
-    case CO:                                                                                    \
-        return mode == 0 ? launch_conv<CO, 0>(ta0, ta1, tb0, tb1, g, bias, out, st)             \
-                         : launch_conv<CO, 1>(ta0, ta1, tb0, tb1, g, bias, out, st);
+    const int cmax = c0 > c1 ? c0 : c1;
+#define CTGB_CONV_CM(CO, CM)                                                                      \
+    if (cmax == CM)                                                                              \
+        return mode == 0 ? launch_conv<CO, CM, 0>(ta0, ta1, tb0, tb1, g, bias, out, st)          \
+                         : launch_conv<CO, CM, 1>(ta0, ta1, tb0, tb1, g, bias, out, st);
+#define CTGB_CONV_CASE(CO)   \
+    case CO:                 \
+        CTGB_CONV_CM(CO, 16) \
+        CTGB_CONV_CM(CO, 32) \
+        CTGB_CONV_CM(CO, 64) \
+        break;
     switch (cout) {
         CTGB_CONV_CASE(16)
         CTGB_CONV_CASE(32)
@@ -554,6 +563,7 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
         CTGB_CONV_CASE(96)
     }
 #undef CTGB_CONV_CASE
+#undef CTGB_CONV_CM
     return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: unsupported output channels");
 }
 

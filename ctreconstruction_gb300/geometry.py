@@ -98,8 +98,8 @@ class ReconstructionParams:
             raise ValueError("pixel and voxel spacings must be positive")
         if self.DetectorShape not in ('Flat', 'Curved'):
             raise ValueError("Detector shape is not supported: %r" % self.DetectorShape)
-        if self.Method != 'Distance':
-            raise ValueError("Method %r is not supported (the reference implements 'Distance' only)" % self.Method)
+        if self.Method not in ('Distance', 'Ray'):
+            raise ValueError("Method must be 'Distance' or 'Ray', got %r" % self.Method)
         if self.flavour not in ('numba', 'pycuda'):
             raise ValueError("flavour must be 'numba' or 'pycuda'")
         if self.sdd <= 0:
