@@ -236,7 +236,7 @@ bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj,
 #endif
 constexpr int kBiZ = CTGB_BI_Z;   // z voxels per thread
 #ifndef CTGB_BI_BLOCKS
-#define CTGB_BI_BLOCKS 6
+#define CTGB_BI_BLOCKS 8
 #endif
 constexpr int kBiBlocks = CTGB_BI_BLOCKS;   // resident CTAs per SM the register budget is sized for
 
@@ -726,7 +726,10 @@ __global__ void matched_integrate_kernel(const float *__restrict__ T, const floa
 
 constexpr int kMC = 6;   // detector columns kept per (voxel column, view); more -> per-voxel path
 
-__global__ void __launch_bounds__(kBpTileX * kBpTileY, 4)
+#ifndef CTGB_MI_BLOCKS
+#define CTGB_MI_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(kBpTileX * kBpTileY, CTGB_MI_BLOCKS)
 bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
                         const float *__restrict__ proj, float *__restrict__ vol, int view0, int nviews, float scale,
                         int accumulate) {
@@ -828,20 +831,26 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             continue;
         }
         if (!live) continue;
+        // Voxel j spans row coordinates [r_j, r_{j+1}] (r_j = al + (l0 + j) be):
+        // consecutive voxels share a boundary, so each of the kMZ + 1
+        // boundaries is clamped to [0, nv] and looked up once, and voxel j
+        // takes e(r_{j+1}) - e(r_j) with e(r) = C + frac * y', signed by the
+        // orientation of be.
 #pragma unroll
         for (int m = 0; m < kMC; ++m) {
             if (m >= ncol) break;
             const float2 *__restrict__ colp = IQ + cc[m];
+            const float w = be[m] > 0.0f ? wcol[m] : -wcol[m];
+            float eprev = 0.0f;
 #pragma unroll
-            for (int j = 0; j < kMZ; ++j) {
-                const float ra = fmaf((float)(l0 + j), be[m], al[m]);
-                const float rb = ra + be[m];
-                const float lo = fminf(fmaxf(fminf(ra, rb), 0.0f), fnv), hi = fminf(fmaxf(fmaxf(ra, rb), 0.0f), fnv);
-                float flo, fhi;
-                const int mlo = floor_split(lo, &flo), mhi = floor_split(hi, &fhi);
-                const float2 a = __ldg(colp + (long long)mlo * nu), b = __ldg(colp + (long long)mhi * nu);
-                const float integ_v = fmaf(b.y, hi - fhi, b.x) - fmaf(a.y, lo - flo, a.x);
-                acc[j] = fmaf(integ_v, wcol[m], acc[j]);
+            for (int j = 0; j <= kMZ; ++j) {
+                const float r = fminf(fmaxf(fmaf((float)(l0 + j), be[m], al[m]), 0.0f), fnv);
+                float fr;
+                const int mr = floor_split(r, &fr);
+                const float2 a = __ldg(colp + (long long)mr * nu);
+                const float e = fmaf(a.y, r - fr, a.x);
+                if (j > 0) acc[j - 1] = fmaf(e - eprev, w, acc[j - 1]);
+                eprev = e;
             }
         }
     }

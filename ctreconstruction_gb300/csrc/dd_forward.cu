@@ -140,9 +140,20 @@ __global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restr
 // voxels, are integrated cell by cell from global memory (compact, rare path).
 constexpr int kTU = 32, kTR = 16, kBoxX = 64, kBoxZ = 8, kPZ = 32, kPX = kBoxX;
 
+// Patch buffers per CTA: 2 overlaps each slice's TMA with the previous
+// slice's compute inside the warp; 1 halves shared memory so twice as many
+// warps are resident and hide the load latency across warps instead.
+#ifndef CTGB_FWD_BUFS
+#define CTGB_FWD_BUFS 1
+#endif
+constexpr int kFwdBufs = CTGB_FWD_BUFS;
+
 struct FwdTmaSmem {
-    float buf[2][kPZ][kPX];
-    float spill[kTR][kTU];      // per-slice row values of the fallback path
+    float buf[kFwdBufs][kPZ][kPX];
+    float bj[kTR + 1];          // the tile's row boundaries (same for every lane)
+    // per-slice row values of the fallback path; with one patch buffer they
+    // live in it (no copy is in flight while a slice is computed)
+    float spill[kFwdBufs == 1 ? 1 : kTR][kTU];
     uint64_t bar[2];
 };
 
@@ -209,8 +220,11 @@ __device__ __forceinline__ void sweep_tile(const float *patch, int lb, const flo
     sweep_rows2<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
 }
 
+#ifndef CTGB_FWD_MINB
+#define CTGB_FWD_MINB 24
+#endif
 template <bool XD, bool TMA>
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(32, CTGB_FWD_MINB)
 dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
                       const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0, int vbase,
                       int ntu, int *status) {
@@ -251,9 +265,13 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     const float invD = 1.0f / (Sa - Pa[cc]);
     const float t1 = (Sb - Pb[cc]) * invD;
     const float A = (Sz - pzp[0]) * inv_dz;
-    float Bj[kTR + 1];
-#pragma unroll
-    for (int j = 0; j <= kTR; ++j) Bj[j] = (Sz - Bzr[min(r0 + j, nv)]) * inv_dz;
+    // Row boundaries in shared memory: one copy per warp instead of kTR + 1
+    // registers per lane (broadcast reads).
+    float *Bj = sm.bj;
+    float *spill_rows = kFwdBufs == 1 ? &sm.buf[0][0][0] : &sm.spill[0][0];
+    static_assert(kTR * kTU <= kPZ * kPX, "fallback rows must fit the patch buffer");
+    if (lane <= kTR) Bj[lane] = (Sz - Bzr[min(r0 + lane, nv)]) * inv_dz;
+    __syncwarp();
     float rowspan_max = 0.0f;
 #pragma unroll
     for (int j = 0; j < kTR; ++j) rowspan_max = fmaxf(rowspan_max, fabsf(Bj[j + 1] - Bj[j]));
@@ -287,7 +305,7 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     // Zero both buffers once so that taps past the loaded boxes read finite zeros.
     {
         float4 *z = reinterpret_cast<float4 *>(&sm.buf[0][0][0]);
-        for (int i = lane; i < 2 * kPZ * kPX / 4; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = lane; i < kFwdBufs * kPZ * kPX / 4; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncwarp();
 
@@ -310,9 +328,9 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     TileWindow wcur = window(0);
     issue(0, wcur, 0);
     for (int s = 0; s < nA; ++s) {
-        const int b = s & 1;
+        const int b = kFwdBufs == 2 ? (s & 1) : 0;
         TileWindow wnext;
-        if (s + 1 < nA) {
+        if (kFwdBufs == 2 && s + 1 < nA) {
             wnext = window(s + 1);
             issue(s + 1, wnext, b ^ 1);
         }
@@ -373,19 +391,23 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
                             hx += __ldg(row + k * st_k) * (fminf((float)(k + 1), hi) - fmaxf((float)k, lo));
                         v += hx * wz;
                     }
-                    sm.spill[j][lane] = v;
+                    spill_rows[j * kTU + lane] = v;
                 }
                 __syncwarp();
 #pragma unroll
-                for (int j = 0; j < kTR; ++j) acc[j] = fmaf(sm.spill[j][lane], g, acc[j]);
+                for (int j = 0; j < kTR; ++j) acc[j] = fmaf(spill_rows[j * kTU + lane], g, acc[j]);
             }
         }
         __syncwarp();
+        if (kFwdBufs == 1 && s + 1 < nA) {
+            wnext = window(s + 1);
+            issue(s + 1, wnext, 0);
+        }
         wcur = wnext;
     }
     if (failed) {
         // Let copies still in flight land before the CTA exits (bounded).
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < kFwdBufs; ++b)
             if ((pending_bits >> b) & 1u) mbar_wait(&sm.bar[b], (phase_bits >> b) & 1u, status);
         return;
     }
