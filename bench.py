@@ -298,17 +298,21 @@ def run_ours(args):
         matched = {"backproject_matched_ms": mm,
                    "pair_value": vv / ((kern["forward"] + kern["transpose"] + mm) / 1e3) / 1e9}
 
-    # end to end through the public API with host arrays (copies inside the timed region)
+    # end to end through the public API with host data (copies inside the
+    # timed region): the volume in pinned host memory goes in, the projections
+    # come back to pinned host memory after forward(), go in again for
+    # backward(), and the volume comes back.
     host_vol = vol.cpu().numpy()
+    pinned_vol = torch.from_numpy(host_vol).pin_memory()
     R = Reconstruction(params, device=dev)
     e2e_steps = max(1, min(args.steps, 3))
-    R.image = host_vol
+    R.image = pinned_vol
     R.forward()
     R.backward()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        R.image = host_vol
+        R.image = pinned_vol
         R.forward()
         R.backward()
     barrier()

@@ -30,9 +30,13 @@ class ErrorDescription(Exception):
 
 def _to_device(a, device):
     if isinstance(a, torch.Tensor):
-        t = a.to(device=device, dtype=torch.float32)
+        t = a.to(device=device, dtype=torch.float32, non_blocking=bool(not a.is_cuda and a.is_pinned()))
         return t.contiguous()
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(device, non_blocking=False)
+
+
+def _on_host(a):
+    return not (isinstance(a, torch.Tensor) and a.is_cuda)
 
 
 class Reconstruction:
@@ -89,6 +93,20 @@ class Reconstruction:
         else:
             self.proj = np.ascontiguousarray(np.flip(self.proj, axis=axis))
 
+    # -- host results ---------------------------------------------------------------
+    def _to_host(self, t, src, key):
+        """Result of a call whose input was on the host: NumPy in -> NumPy out
+        (as the reference); a CPU tensor in -> a pinned CPU tensor out, copied
+        asynchronously into a buffer the object reuses for that attribute
+        (copy it before the next call to keep it)."""
+        if isinstance(src, torch.Tensor):
+            cache = self.__dict__.setdefault("_pinned", {})
+            out = _pinned_like(cache, key, t)
+            out.copy_(t, non_blocking=True)
+            torch.cuda.current_stream(t.device).synchronize()
+            return out
+        return _host(t)
+
     # -- projectors ----------------------------------------------------------------
     def forward(self):
         """self.proj = forward projection of self.image: DD (distance_forward)
@@ -96,10 +114,11 @@ class Reconstruction:
         the reference, Reconstruction_numba.py:799-801)."""
         if self.Method not in ('Distance', 'Ray'):
             return
-        host = not isinstance(self.image, torch.Tensor)
-        vol = _to_device(self.image, self.projector.device)
+        src = self.image
+        host = _on_host(src)
+        vol = _to_device(src, self.projector.device)
         proj = self.projector.forward(vol) if self.Method == 'Distance' else self.projector.ray_forward(vol)
-        self.proj = _host(proj) if host else proj
+        self.proj = self._to_host(proj, src, "proj") if host else proj
 
     def backward(self):
         """self.image = FDK-weighted DD backprojection of self.proj * dtheta
@@ -108,20 +127,30 @@ class Reconstruction:
         dtheta."""
         if self.Method not in ('Distance', 'Ray'):
             return
-        host = not isinstance(self.proj, torch.Tensor)
-        q = _to_device(self.proj, self.projector.device)
+        src = self.proj
+        host = _on_host(src)
+        q = _to_device(src, self.projector.device)
         if self.Method == 'Distance':
             vol = self.projector.backproject_fdk(q)
         else:
             vol = self.projector.ray_backproject(q, scale=self.projector.params.dtheta)
-        self.image = _host(vol) if host else vol
+        self.image = self._to_host(vol, src, "image") if host else vol
 
     def Filtering(self):
         """In-place cosine pre-weight and ramp filter of self.proj (Filtering)."""
-        host = not isinstance(self.proj, torch.Tensor)
-        q = _to_device(self.proj, self.projector.device)
+        src = self.proj
+        host = _on_host(src)
+        q = _to_device(src, self.projector.device)
         self.projector.filter(q, self.FilterType, self.cutoff)
-        self.proj = _host(q) if host else q
+        self.proj = self._to_host(q, src, "proj") if host else q
+
+
+def _pinned_like(cache, key, t):
+    buf = cache.get(key)
+    if buf is None or buf.shape != t.shape:
+        buf = torch.empty(t.shape, dtype=torch.float32, pin_memory=True)
+        cache[key] = buf
+    return buf
 
 
 def _host(a):

@@ -239,3 +239,17 @@ def test_ray_method_through_reconstruction(cuda):
     lhs = torch.sum(P.ray_forward(a).double() * b.double()).item()
     rhs = torch.sum(a.double() * P.ray_backproject(b).double()).item()
     assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+
+
+def test_reconstruction_pinned_host_tensors(cuda):
+    """CPU (pinned) tensors in -> pinned CPU tensors out, same values as the
+    NumPy round trip."""
+    p, flavour, d = load_golden("numba_basic")
+    R = Reconstruction(p, flavour=flavour)
+    R.image = torch.from_numpy(d["image"].copy()).pin_memory()
+    R.forward()
+    assert isinstance(R.proj, torch.Tensor) and not R.proj.is_cuda and R.proj.is_pinned()
+    assert rel_err(R.proj.numpy(), d["forward"]) < RTOL
+    R.proj = torch.from_numpy(d["proj"].copy()).pin_memory()
+    R.backward()
+    assert not R.image.is_cuda and rel_err(R.image.numpy(), d["backward"]) < RTOL
