@@ -69,7 +69,8 @@ bool ctgb_make_tmap_bf16(CUtensorMap *map, const void *base, int rank, const uin
     if (reinterpret_cast<uintptr_t>(base) % 16) return false;
     const uint32_t inner = box[0] * 2;
     CUtensorMapSwizzle sw;
-    if (inner == 32) sw = CU_TENSOR_MAP_SWIZZLE_32B;
+    if (inner == 16) sw = CU_TENSOR_MAP_SWIZZLE_NONE;
+    else if (inner == 32) sw = CU_TENSOR_MAP_SWIZZLE_32B;
     else if (inner == 64) sw = CU_TENSOR_MAP_SWIZZLE_64B;
     else if (inner == 128) sw = CU_TENSOR_MAP_SWIZZLE_128B;
     else return false;

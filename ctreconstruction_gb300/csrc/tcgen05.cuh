@@ -34,6 +34,18 @@ __device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, uint32_t row_
     return d;
 }
 
+// Descriptor of a K-major operand in the unswizzled (interleaved) layout:
+// 8 x 16-byte core matrices whose 8 rows are 16 bytes apart, core matrices
+// adjacent in K `lbo` bytes apart and 8-row groups `sbo` bytes apart; the
+// start address only needs 16-byte alignment, so a tile may begin at any row.
+__device__ __forceinline__ uint64_t umma_smem_desc_interleaved(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1u << 46;
+    return d;                                   // layout type 0: no swizzle
+}
+
 __host__ __device__ constexpr uint32_t umma_idesc_bf16_f32(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }

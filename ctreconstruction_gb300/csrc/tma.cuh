@@ -32,6 +32,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Bounded wait for the phase with the given parity; false on timeout (and
 // kDevErrTimeout is or-ed into *status, the library's device status word).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
@@ -77,7 +81,8 @@ bool ctgb_make_tmap_3d(CUtensorMap *map, const float *base, const uint64_t dims[
 
 // Host: a bf16 tiled tensor map of `rank` dims (innermost first, dense
 // strides), with the shared-memory swizzle whose span equals the box's inner
-// extent in bytes (32, 64 or 128).  Out-of-bounds elements load as zeros.
+// extent in bytes (32, 64 or 128; a 16-byte inner extent is unswizzled).
+// Out-of-bounds elements load as zeros.
 bool ctgb_make_tmap_bf16(CUtensorMap *map, const void *base, int rank, const uint64_t *dims, const uint32_t *box);
 
 // Host: device address of the library's status word on the current device

@@ -172,6 +172,196 @@ conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant_
     }
 }
 
+// ---- x-tap reuse for rows of 128 voxels ---------------------------------------
+//
+// When W is a multiple of 128 a tile is one run of 128 voxels along x, and the
+// three x taps of a (dz, dy) pair read the same input row shifted by one
+// voxel.  conv3d_tc_dx_kernel loads that row once per (dz, dy) — 130 voxels
+// (x0 - 1 .. x0 + 128), as 8-channel boxes into the unswizzled K-major
+// layout, where every 16-byte voxel row stands alone — and starts the A
+// operand of tap dx at row dx (a 16-byte offset of the descriptor).  Per
+// tile: 9 input loads and 27 weight blocks instead of 27 and 27.
+//
+// The kernel is persistent and warp-specialised: warp 0 issues the TMA loads
+// of tile after tile into a ring of stages, warp 1 issues the MMAs into one
+// of two TMEM accumulators, and warps 2-5 drain the other accumulator
+// (tcgen05.ld, bias/ReLU, stores), so a tile's epilogue overlaps the next
+// tile's loads and MMAs.
+template <int COUT, int CMAX>
+struct ConvDxCfg {
+    static constexpr int kRows = kCvM + 2;
+    static constexpr int kChunk = ((kRows * 16 + 127) / 128) * 128;        // one 8-channel slab of 130 rows
+    static constexpr int kABytes = (((CMAX / 8) * kChunk + 1023) / 1024) * 1024;
+    static constexpr int kBTap = ((COUT * CMAX * 2 + 1023) / 1024) * 1024;
+    static constexpr int kStage = kABytes + 3 * kBTap;
+    static constexpr int kStages = (65536 / kStage) < 2 ? 2 : ((65536 / kStage) > 6 ? 6 : 65536 / kStage);
+    static constexpr int kAccCols = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);   // one accumulator
+    static constexpr int kTmemCols = 2 * kAccCols;
+    static constexpr int kSmem = kStages * kStage + 256 + 1024;
+};
+constexpr int kDxThreads = 192;   // producer warp, MMA warp, 4 epilogue warps
+
+template <int COUT, int CMAX, int EPI>
+__global__ void __launch_bounds__(kDxThreads, 1)
+conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
+                    const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1,
+                    const ConvGeom g, const float *__restrict__ bias, void *__restrict__ out, int *status) {
+    using Cfg = ConvDxCfg<COUT, CMAX>;
+    extern __shared__ uint8_t smraw[];
+    const uint32_t raw = smem_addr(smraw);
+    uint8_t *base = smraw + (((raw + 1023u) & ~1023u) - raw);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + Cfg::kStages * Cfg::kStage);
+    uint64_t *empty = full + Cfg::kStages;
+    uint64_t *acc_full = empty + Cfg::kStages;     // [2]: MMAs of a tile done
+    uint64_t *acc_empty = acc_full + 2;            // [2]: epilogue has read the accumulator
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = g.W / kCvM;
+    const int ntiles = g.N * g.D * g.H * tiles_x;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < Cfg::kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 128);
+        }
+        *failed = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(tslot, Cfg::kTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int steps_per_tile = 9 * g.nseg;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // TMA producer: every tile's (dz, dy) x segment steps, back to back.
+            int i = 0;
+            for (int tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x) {
+                int t = tile;
+                const int x0 = (t % tiles_x) * kCvM;
+                t /= tiles_x;
+                const int hh = t % g.H;
+                t /= g.H;
+                const int d = t % g.D, n = t / g.D;
+                for (int k = 0; k < steps_per_tile; ++k, ++i) {
+                    const int s = i % Cfg::kStages;
+                    if (i >= Cfg::kStages && !mbar_wait(&empty[s], ((i / Cfg::kStages) - 1) & 1, status)) {
+                        *failed = 1;
+                        break;
+                    }
+                    const int pair = k / g.nseg, seg = k - pair * g.nseg;
+                    const int c = seg ? g.c1 : g.c0;
+                    uint8_t *A = base + s * Cfg::kStage;
+                    uint8_t *B = A + Cfg::kABytes;
+                    mbar_arrive_expect_tx(&full[s], (uint32_t)((c / 8) * Cfg::kRows * 16 + 3 * COUT * c * 2));
+                    const int dz = pair / 3 - 1, dy = pair % 3 - 1;
+                    for (int ch = 0; ch < c / 8; ++ch)
+                        tma_load_5d(A + ch * Cfg::kChunk, seg ? &ta1 : &ta0, ch * 8, x0 - 1, hh + dy, d + dz, n,
+                                    &full[s]);
+                    for (int dx = 0; dx < 3; ++dx)
+                        tma_load_2d(B + dx * Cfg::kBTap, seg ? &tb1 : &tb0, 0, (pair * 3 + dx) * COUT, &full[s]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer: accumulator j & 1 for the CTA's j-th tile.
+            constexpr uint32_t idesc = umma_idesc_bf16_f32(kCvM, COUT);
+            int i = 0, j = 0;
+            for (int tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x, ++j) {
+                const int b = j & 1, u = j >> 1;
+                if (u > 0 && !mbar_wait(&acc_empty[b], (u - 1) & 1, status)) {
+                    *failed = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t dacc = tmem + (uint32_t)(b * Cfg::kAccCols);
+                bool ok = true;
+                for (int k = 0; k < steps_per_tile; ++k, ++i) {
+                    const int s = i % Cfg::kStages;
+                    if (!mbar_wait(&full[s], (i / Cfg::kStages) & 1, status)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const int seg = k % g.nseg;
+                    const uint32_t c = (uint32_t)(seg ? g.c1 : g.c0);
+                    const uint32_t a_addr = smem_addr(base + s * Cfg::kStage), b_addr = a_addr + Cfg::kABytes;
+                    for (uint32_t dx = 0; dx < 3; ++dx)
+                        for (uint32_t kk = 0; kk < c / 16; ++kk)
+                            umma_bf16(dacc,
+                                      umma_smem_desc_interleaved(a_addr + 16u * dx + 2u * kk * Cfg::kChunk,
+                                                                 Cfg::kChunk, 128u),
+                                      umma_smem_desc(b_addr + dx * Cfg::kBTap + 32u * kk, c * 2u), idesc,
+                                      (k > 0 || dx > 0 || kk > 0) ? 1u : 0u);
+                    umma_commit(&empty[s]);
+                }
+                if (!ok) {
+                    *failed = 1;
+                    break;
+                }
+                umma_commit(&acc_full[b]);
+            }
+        }
+    } else {
+        // Epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. +31.
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        int j = 0;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+            const int b = j & 1, u = j >> 1;
+            const bool got = mbar_wait(&acc_full[b], u & 1, status);
+            tc_fence_after();
+            if (!__all_sync(0xffffffffu, got && !*failed)) break;
+            int t = tile;
+            const int x0 = (t % tiles_x) * kCvM;
+            t /= tiles_x;
+            const int hh = t % g.H;
+            t /= g.H;
+            const int d = t % g.D, n = t / g.D;
+            const long long vox = (((long long)n * g.D + d) * g.H + hh) * g.W + x0 + row;
+            const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * Cfg::kAccCols);
+#pragma unroll
+            for (int cb = 0; cb < COUT; cb += 16) {
+                float v[16];
+                tmem_ld16(tbase + (uint32_t)cb, v);
+                if (EPI == 0) {
+                    uint32_t p[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        p[q] = pack_bf16x2(fmaxf(v[2 * q] + bias[cb + 2 * q], 0.0f),
+                                           fmaxf(v[2 * q + 1] + bias[cb + 2 * q + 1], 0.0f));
+                    uint4 *o = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + vox * COUT + cb);
+                    o[0] = make_uint4(p[0], p[1], p[2], p[3]);
+                    o[1] = make_uint4(p[4], p[5], p[6], p[7]);
+                } else {
+                    float4 *o = reinterpret_cast<float4 *>(static_cast<float *>(out) + vox * COUT + cb);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acc_empty[b]);
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, Cfg::kTmemCols);
+    }
+}
+
 // ---- CUDA-core passes -------------------------------------------------------
 
 // x fp32 [N][V] -> bf16 [N][V][16]: channel 0 = x / scale[n], the rest 0.
@@ -500,6 +690,44 @@ static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUten
     return CTGB_OK;
 }
 
+template <int COUT, int CMAX, int EPI>
+static int launch_conv_dx(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
+                          const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
+    using Cfg = ConvDxCfg<COUT, CMAX>;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_dx_kernel<COUT, CMAX, EPI>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
+        attr = true;
+    }
+    int *status = ctgb_status_ptr();
+    if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
+    const long long tiles = (long long)g.N * g.D * g.H * (g.W / kCvM);
+    if (tiles > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "conv3d: too many tiles");
+    // Persistent grid: as many CTAs as fit on the GPU at once (shared memory
+    // and TMEM bound), never more than the tiles.
+    static int resident = 0;
+    if (!resident) {
+        int sms = 0, smem_sm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        // CTAs per SM: shared memory (1 KB reserved per CTA), TMEM columns,
+        // threads; registers (under 64 per thread) never bind first here.
+        int per_sm = smem_sm / (Cfg::kSmem + 1024);
+        if (per_sm > 512 / Cfg::kTmemCols) per_sm = 512 / Cfg::kTmemCols;
+        if (per_sm > 2048 / kDxThreads) per_sm = 2048 / kDxThreads;
+        resident = (per_sm < 1 ? 1 : per_sm) * (sms < 1 ? 1 : sms);
+    }
+    const int grid = (int)(tiles < resident ? tiles : resident);
+    conv3d_tc_dx_kernel<COUT, CMAX, EPI><<<grid, kDxThreads, Cfg::kSmem, st>>>(a0, a1, b0, b1, g, bias, out,
+                                                                              status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d_tc_dx_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
 }  // namespace ctgb
 
 using namespace ctgb;
@@ -523,10 +751,14 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     const int r = 128 / wb;
     if (h % r) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: H must be a multiple of %d for W = %d", r, w);
     ConvGeom g{n, d, h, w, wb, r, c0, c1, c1 ? 2 : 1};
+    // Rows of 128 voxels take the x-tap reuse kernel: input boxes of 8
+    // channels x 130 voxels (unswizzled), weight boxes as before.
+    const bool dxr = (w % kCvM) == 0;
     CUtensorMap ta0, ta1, tb0, tb1;
     {
         const uint64_t dims[5] = {(uint64_t)c0, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {(uint32_t)c0, (uint32_t)wb, (uint32_t)r, 1u, 1u};
+        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c0, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb, (uint32_t)r,
+                                 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c0, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c0, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta0, x0, 5, dims, box) || !ctgb_make_tmap_bf16(&tb0, w0, 2, wd, wbx))
@@ -534,7 +766,8 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     }
     if (c1) {
         const uint64_t dims[5] = {(uint64_t)c1, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {(uint32_t)c1, (uint32_t)wb, (uint32_t)r, 1u, 1u};
+        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c1, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb, (uint32_t)r,
+                                 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c1, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c1, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta1, x1, 5, dims, box) || !ctgb_make_tmap_bf16(&tb1, w1, 2, wd, wbx))
@@ -546,6 +779,9 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int cmax = c0 > c1 ? c0 : c1;
 #define CTGB_CONV_CM(CO, CM)                                                                      \
+    if (cmax == CM && dxr)                                                                       \
+        return mode == 0 ? launch_conv_dx<CO, CM, 0>(ta0, ta1, tb0, tb1, g, bias, out, st)       \
+                         : launch_conv_dx<CO, CM, 1>(ta0, ta1, tb0, tb1, g, bias, out, st);     \
     if (cmax == CM)                                                                              \
         return mode == 0 ? launch_conv<CO, CM, 0>(ta0, ta1, tb0, tb1, g, bias, out, st)          \
                          : launch_conv<CO, CM, 1>(ta0, ta1, tb0, tb1, g, bias, out, st);

@@ -41,7 +41,13 @@ CONFIGS = [
     (32, 16, 16, (1, 4, 32, 64)),
     (16, 0, 48, (1, 4, 32, 64)),
     (64, 0, 96, (1, 2, 8, 16)),
+    # rows of 128 voxels: the x-tap reuse kernel
     (16, 0, 16, (1, 2, 3, 256)),
+    (32, 0, 32, (1, 2, 2, 128)),
+    (64, 32, 32, (1, 2, 2, 128)),
+    (32, 16, 48, (1, 2, 2, 256)),
+    (64, 0, 96, (1, 1, 2, 128)),
+    (16, 0, 64, (2, 2, 2, 128)),
 ]
 
 
