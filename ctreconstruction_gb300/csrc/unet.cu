@@ -172,49 +172,71 @@ conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant_
     }
 }
 
-// ---- x-tap reuse for rows of 128 voxels ---------------------------------------
+// ---- tap reuse for rows of 128 voxels ------------------------------------------
 //
-// When W is a multiple of 128 a tile is one run of 128 voxels along x, and the
-// three x taps of a (dz, dy) pair read the same input row shifted by one
-// voxel.  conv3d_tc_dx_kernel loads that row once per (dz, dy) — 130 voxels
-// (x0 - 1 .. x0 + 128), as 8-channel boxes into the unswizzled K-major
-// layout, where every 16-byte voxel row stands alone — and starts the A
-// operand of tap dx at row dx (a 16-byte offset of the descriptor).  Per
-// tile: 9 input loads and 27 weight blocks instead of 27 and 27.
+// When W is a multiple of 128 a tile is one run of 128 voxels along x.  For
+// one dz plane, the nine (dy, dx) taps read three input rows (y - 1 .. y + 1),
+// each shifted by one voxel per dx.  conv3d_tc_dx_kernel loads those rows
+// once per dz — 3 x 130 voxels (x0 - 1 .. x0 + 128), as 8-channel boxes into
+// the unswizzled K-major layout, where every 16-byte voxel row stands alone —
+// and starts the A operand of tap (dy, dx) at row dy * 130 + dx (a 16-byte
+// multiple of the descriptor's start address).  When the layer's weights fit
+// (<= 64 KB) they are loaded once per CTA and stay in shared memory;
+// otherwise each stage also carries its nine weight blocks.
 //
 // The kernel is persistent and warp-specialised: warp 0 issues the TMA loads
 // of tile after tile into a ring of stages, warp 1 issues the MMAs into one
 // of two TMEM accumulators, and warps 2-5 drain the other accumulator
 // (tcgen05.ld, bias/ReLU, stores), so a tile's epilogue overlaps the next
 // tile's loads and MMAs.
-template <int COUT, int CMAX>
+template <int COUT, int CMAX, bool RES>
 struct ConvDxCfg {
     static constexpr int kRows = kCvM + 2;
-    static constexpr int kChunk = ((kRows * 16 + 127) / 128) * 128;        // one 8-channel slab of 130 rows
+    static constexpr int kPlane = kRows * 16;                                    // one dy row of 8 channels
+    static constexpr int kChunk = ((3 * kPlane + 127) / 128) * 128;              // three dy rows
     static constexpr int kABytes = (((CMAX / 8) * kChunk + 1023) / 1024) * 1024;
-    static constexpr int kBTap = ((COUT * CMAX * 2 + 1023) / 1024) * 1024;
-    static constexpr int kStage = kABytes + 3 * kBTap;
-    static constexpr int kStages = (65536 / kStage) < 2 ? 2 : ((65536 / kStage) > 6 ? 6 : 65536 / kStage);
+    static constexpr int kBTap = COUT * CMAX * 2;                                // one tap's weight block
+    static constexpr int kStage = kABytes + (RES ? 0 : ((9 * kBTap + 1023) / 1024) * 1024);
+    static constexpr int kBudget = 49152;
+    static constexpr int kStages = (kBudget / kStage) < 2 ? 2 : ((kBudget / kStage) > 6 ? 6 : kBudget / kStage);
     static constexpr int kAccCols = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);   // one accumulator
     static constexpr int kTmemCols = 2 * kAccCols;
-    static constexpr int kSmem = kStages * kStage + 256 + 1024;
+    static constexpr int kWMax = 65536;                                          // resident weights, at most
+    static constexpr int kSmemFixed = kStages * kStage + 256 + 1024;
 };
 constexpr int kDxThreads = 192;   // producer warp, MMA warp, 4 epilogue warps
+constexpr int kDxSmemLimit = 227 * 1024;
 
-template <int COUT, int CMAX, int EPI>
+// Host: whether the tap-reuse kernel's shared memory fits for this shape (the
+// same sizes as ConvDxCfg, with the resident-weight choice of launch_conv_dx).
+static bool dx_fits(int cout, int cmax, int nseg) {
+    const int chunk = ((3 * (kCvM + 2) * 16 + 127) / 128) * 128;
+    const int abytes = (((cmax / 8) * chunk + 1023) / 1024) * 1024;
+    const int btap = cout * cmax * 2;
+    const bool res = nseg * 27 * btap <= 65536;
+    const int stage = abytes + (res ? 0 : ((9 * btap + 1023) / 1024) * 1024);
+    int stages = 49152 / stage;
+    stages = stages < 2 ? 2 : (stages > 6 ? 6 : stages);
+    return (res ? 65536 : 0) + stages * stage + 256 + 1024 <= kDxSmemLimit;
+}
+
+template <int COUT, int CMAX, int EPI, bool RES>
 __global__ void __launch_bounds__(kDxThreads, 1)
 conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
                     const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1,
-                    const ConvGeom g, const float *__restrict__ bias, void *__restrict__ out, int *status) {
-    using Cfg = ConvDxCfg<COUT, CMAX>;
+                    const ConvGeom g, int wres, const float *__restrict__ bias, void *__restrict__ out,
+                    int *status) {
+    using Cfg = ConvDxCfg<COUT, CMAX, RES>;
     extern __shared__ uint8_t smraw[];
     const uint32_t raw = smem_addr(smraw);
-    uint8_t *base = smraw + (((raw + 1023u) & ~1023u) - raw);
+    uint8_t *wbase = smraw + (((raw + 1023u) & ~1023u) - raw);     // resident weights (wres bytes)
+    uint8_t *base = wbase + wres;                                   // stage ring
     uint64_t *full = reinterpret_cast<uint64_t *>(base + Cfg::kStages * Cfg::kStage);
     uint64_t *empty = full + Cfg::kStages;
     uint64_t *acc_full = empty + Cfg::kStages;     // [2]: MMAs of a tile done
     uint64_t *acc_empty = acc_full + 2;            // [2]: epilogue has read the accumulator
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    uint64_t *wbar = acc_empty + 2;                // resident weights landed
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(wbar + 1);
     volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -230,6 +252,7 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 128);
         }
+        mbar_init(wbar, 1);
         *failed = 0;
         fence_mbar_init();
     }
@@ -238,11 +261,19 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const int steps_per_tile = 9 * g.nseg;
+    const int steps_per_tile = 3 * g.nseg;
 
     if (warp == 0) {
         if (lane == 0) {
-            // TMA producer: every tile's (dz, dy) x segment steps, back to back.
+            if (RES) {
+                uint32_t bytes = 0;
+                for (int seg = 0; seg < g.nseg; ++seg) bytes += 27u * COUT * (uint32_t)(seg ? g.c1 : g.c0) * 2u;
+                mbar_arrive_expect_tx(wbar, bytes);
+                for (int seg = 0; seg < g.nseg; ++seg)
+                    for (int tap = 0; tap < 27; ++tap)
+                        tma_load_2d(wbase + (seg * 27 + tap) * Cfg::kBTap, seg ? &tb1 : &tb0, 0, tap * COUT, wbar);
+            }
+            // TMA producer: every tile's dz x segment steps, back to back.
             int i = 0;
             for (int tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x) {
                 int t = tile;
@@ -257,17 +288,18 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                         *failed = 1;
                         break;
                     }
-                    const int pair = k / g.nseg, seg = k - pair * g.nseg;
+                    const int dzi = k / g.nseg, seg = k - dzi * g.nseg;
                     const int c = seg ? g.c1 : g.c0;
                     uint8_t *A = base + s * Cfg::kStage;
                     uint8_t *B = A + Cfg::kABytes;
-                    mbar_arrive_expect_tx(&full[s], (uint32_t)((c / 8) * Cfg::kRows * 16 + 3 * COUT * c * 2));
-                    const int dz = pair / 3 - 1, dy = pair % 3 - 1;
+                    mbar_arrive_expect_tx(&full[s], (uint32_t)((c / 8) * 3 * Cfg::kPlane +
+                                                               (RES ? 0 : 9 * COUT * c * 2)));
                     for (int ch = 0; ch < c / 8; ++ch)
-                        tma_load_5d(A + ch * Cfg::kChunk, seg ? &ta1 : &ta0, ch * 8, x0 - 1, hh + dy, d + dz, n,
+                        tma_load_5d(A + ch * Cfg::kChunk, seg ? &ta1 : &ta0, ch * 8, x0 - 1, hh - 1, d + dzi - 1, n,
                                     &full[s]);
-                    for (int dx = 0; dx < 3; ++dx)
-                        tma_load_2d(B + dx * Cfg::kBTap, seg ? &tb1 : &tb0, 0, (pair * 3 + dx) * COUT, &full[s]);
+                    if (!RES)
+                        for (int q = 0; q < 9; ++q)
+                            tma_load_2d(B + q * Cfg::kBTap, seg ? &tb1 : &tb0, 0, (dzi * 9 + q) * COUT, &full[s]);
                 }
             }
         }
@@ -275,16 +307,17 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
         if (lane == 0) {
             // MMA issuer: accumulator j & 1 for the CTA's j-th tile.
             constexpr uint32_t idesc = umma_idesc_bf16_f32(kCvM, COUT);
+            bool ok = !RES || mbar_wait(wbar, 0, status);
+            const uint32_t w_addr = smem_addr(wbase);
             int i = 0, j = 0;
-            for (int tile = blockIdx.x; tile < ntiles && !*failed; tile += gridDim.x, ++j) {
+            for (int tile = blockIdx.x; ok && tile < ntiles && !*failed; tile += gridDim.x, ++j) {
                 const int b = j & 1, u = j >> 1;
                 if (u > 0 && !mbar_wait(&acc_empty[b], (u - 1) & 1, status)) {
-                    *failed = 1;
+                    ok = false;
                     break;
                 }
                 tc_fence_after();
                 const uint32_t dacc = tmem + (uint32_t)(b * Cfg::kAccCols);
-                bool ok = true;
                 for (int k = 0; k < steps_per_tile; ++k, ++i) {
                     const int s = i % Cfg::kStages;
                     if (!mbar_wait(&full[s], (i / Cfg::kStages) & 1, status)) {
@@ -292,24 +325,27 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                         break;
                     }
                     tc_fence_after();
-                    const int seg = k % g.nseg;
+                    const int dzi = k / g.nseg, seg = k - dzi * g.nseg;
                     const uint32_t c = (uint32_t)(seg ? g.c1 : g.c0);
                     const uint32_t a_addr = smem_addr(base + s * Cfg::kStage), b_addr = a_addr + Cfg::kABytes;
-                    for (uint32_t dx = 0; dx < 3; ++dx)
+                    for (uint32_t q = 0; q < 9; ++q) {
+                        const uint32_t dy = q / 3u, dx = q % 3u;
+                        const uint32_t bt = RES ? w_addr + (uint32_t)(seg * 27 + dzi * 9) * Cfg::kBTap + q * Cfg::kBTap
+                                                : b_addr + q * Cfg::kBTap;
                         for (uint32_t kk = 0; kk < c / 16; ++kk)
                             umma_bf16(dacc,
-                                      umma_smem_desc_interleaved(a_addr + 16u * dx + 2u * kk * Cfg::kChunk,
+                                      umma_smem_desc_interleaved(a_addr + dy * Cfg::kPlane + 16u * dx +
+                                                                     2u * kk * Cfg::kChunk,
                                                                  Cfg::kChunk, 128u),
-                                      umma_smem_desc(b_addr + dx * Cfg::kBTap + 32u * kk, c * 2u), idesc,
-                                      (k > 0 || dx > 0 || kk > 0) ? 1u : 0u);
+                                      umma_smem_desc(bt + 32u * kk, c * 2u), idesc,
+                                      (k > 0 || q > 0 || kk > 0) ? 1u : 0u);
+                    }
                     umma_commit(&empty[s]);
                 }
-                if (!ok) {
-                    *failed = 1;
-                    break;
-                }
+                if (!ok) break;
                 umma_commit(&acc_full[b]);
             }
+            if (!ok) *failed = 1;
         }
     } else {
         // Epilogue warps 2-5: warp w reads TMEM lanes 32 (w % 4) .. +31.
@@ -357,6 +393,8 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
+        if (RES && lane == 0 && *failed) mbar_wait(wbar, 0, status);   // resident weight copies have landed
+        __syncwarp();
         tc_fence_after();
         tmem_dealloc(tmem, Cfg::kTmemCols);
     }
@@ -690,14 +728,23 @@ static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUten
     return CTGB_OK;
 }
 
-template <int COUT, int CMAX, int EPI>
-static int launch_conv_dx(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
-                          const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
-    using Cfg = ConvDxCfg<COUT, CMAX>;
+template <int COUT, int CMAX, int EPI, bool RES>
+static int launch_conv_dx_res(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
+                              const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
+    using Cfg = ConvDxCfg<COUT, CMAX, RES>;
+    const int wres = RES ? g.nseg * 27 * Cfg::kBTap : 0;
+    const int smem = wres + Cfg::kSmemFixed;
+    // Largest dynamic shared memory this instantiation can ask for; shapes
+    // that would not fit never get here (ctgb_unet_conv3d routes them to
+    // conv3d_tc_kernel).
+    constexpr int kSmemMax = (RES ? Cfg::kWMax : 0) + Cfg::kSmemFixed;
+    if constexpr (kSmemMax > kDxSmemLimit) {
+        return set_error(CTGB_ERR_ARG, "conv3d: tap-reuse shape above the shared-memory limit");
+    } else {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_dx_kernel<COUT, CMAX, EPI>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
+        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_dx_kernel<COUT, CMAX, EPI, RES>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax);
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
         attr = true;
     }
@@ -705,27 +752,33 @@ static int launch_conv_dx(const CUtensorMap &a0, const CUtensorMap &a1, const CU
     if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
     const long long tiles = (long long)g.N * g.D * g.H * (g.W / kCvM);
     if (tiles > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "conv3d: too many tiles");
-    // Persistent grid: as many CTAs as fit on the GPU at once (shared memory
-    // and TMEM bound), never more than the tiles.
-    static int resident = 0;
-    if (!resident) {
-        int sms = 0, smem_sm = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        // CTAs per SM: shared memory (1 KB reserved per CTA), TMEM columns,
-        // threads; registers (under 64 per thread) never bind first here.
-        int per_sm = smem_sm / (Cfg::kSmem + 1024);
-        if (per_sm > 512 / Cfg::kTmemCols) per_sm = 512 / Cfg::kTmemCols;
-        if (per_sm > 2048 / kDxThreads) per_sm = 2048 / kDxThreads;
-        resident = (per_sm < 1 ? 1 : per_sm) * (sms < 1 ? 1 : sms);
-    }
+    // Persistent grid: as many CTAs as fit on the GPU at once (shared memory,
+    // TMEM and thread bound), never more than the tiles.
+    int sms = 0, smem_sm = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    int per_sm = smem_sm / (smem + 1024);
+    if (per_sm > 512 / Cfg::kTmemCols) per_sm = 512 / Cfg::kTmemCols;
+    if (per_sm > 2048 / kDxThreads) per_sm = 2048 / kDxThreads;
+    const long long resident = (long long)(per_sm < 1 ? 1 : per_sm) * (sms < 1 ? 1 : sms);
     const int grid = (int)(tiles < resident ? tiles : resident);
-    conv3d_tc_dx_kernel<COUT, CMAX, EPI><<<grid, kDxThreads, Cfg::kSmem, st>>>(a0, a1, b0, b1, g, bias, out,
-                                                                              status);
+    conv3d_tc_dx_kernel<COUT, CMAX, EPI, RES><<<grid, kDxThreads, smem, st>>>(a0, a1, b0, b1, g, wres, bias, out,
+                                                                             status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d_tc_dx_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
+    }
+}
+
+template <int COUT, int CMAX, int EPI>
+static int launch_conv_dx(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
+                          const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
+    // Weights resident when they fit the 64 KB budget.
+    const long long wres = (long long)g.nseg * 27 * ConvDxCfg<COUT, CMAX, true>::kBTap;
+    if (wres <= ConvDxCfg<COUT, CMAX, true>::kWMax)
+        return launch_conv_dx_res<COUT, CMAX, EPI, true>(a0, a1, b0, b1, g, bias, out, st);
+    return launch_conv_dx_res<COUT, CMAX, EPI, false>(a0, a1, b0, b1, g, bias, out, st);
 }
 
 }  // namespace ctgb
@@ -751,14 +804,14 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     const int r = 128 / wb;
     if (h % r) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: H must be a multiple of %d for W = %d", r, w);
     ConvGeom g{n, d, h, w, wb, r, c0, c1, c1 ? 2 : 1};
-    // Rows of 128 voxels take the x-tap reuse kernel: input boxes of 8
-    // channels x 130 voxels (unswizzled), weight boxes as before.
-    const bool dxr = (w % kCvM) == 0;
+    // Rows of 128 voxels take the tap reuse kernel: input boxes of 8 channels
+    // x 130 voxels x 3 rows (unswizzled), weight boxes as before.
+    const bool dxr = (w % kCvM) == 0 && dx_fits(cout, c0 > c1 ? c0 : c1, c1 ? 2 : 1);
     CUtensorMap ta0, ta1, tb0, tb1;
     {
         const uint64_t dims[5] = {(uint64_t)c0, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c0, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb, (uint32_t)r,
-                                 1u, 1u};
+        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c0, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
+                                 dxr ? 3u : (uint32_t)r, 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c0, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c0, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta0, x0, 5, dims, box) || !ctgb_make_tmap_bf16(&tb0, w0, 2, wd, wbx))
@@ -766,8 +819,8 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     }
     if (c1) {
         const uint64_t dims[5] = {(uint64_t)c1, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c1, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb, (uint32_t)r,
-                                 1u, 1u};
+        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c1, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
+                                 dxr ? 3u : (uint32_t)r, 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c1, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c1, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta1, x1, 5, dims, box) || !ctgb_make_tmap_bf16(&tb1, w1, 2, wd, wbx))
