@@ -174,50 +174,78 @@ conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant_
 
 // ---- tap reuse for rows of 128 voxels ------------------------------------------
 //
-// When W is a multiple of 128 a tile is one run of 128 voxels along x.  For
-// one dz plane, the nine (dy, dx) taps read three input rows (y - 1 .. y + 1),
-// each shifted by one voxel per dx.  conv3d_tc_dx_kernel loads those rows
-// once per dz — 3 x 130 voxels (x0 - 1 .. x0 + 128), as 8-channel boxes into
-// the unswizzled K-major layout, where every 16-byte voxel row stands alone —
-// and starts the A operand of tap (dy, dx) at row dy * 130 + dx (a 16-byte
-// multiple of the descriptor's start address).  When the layer's weights fit
-// (<= 64 KB) they are loaded once per CTA and stay in shared memory;
-// otherwise each stage also carries its nine weight blocks.
+// When W is a multiple of 128 a tile is R runs of 128 voxels along x, in R
+// consecutive rows y0 .. y0 + R - 1 (R = 4, 2 or 1 by the layer's channel
+// counts; rows past H are computed from zero fill and not stored).  For one
+// dz plane, the 9 R (row, dy, dx) products read R + 2 input rows
+// (y0 - 1 .. y0 + R), each shifted by one voxel per dx.
+// conv3d_tc_dx_kernel loads those rows once per dz and segment — one TMA box
+// of (R + 2) x 130 whole voxels (x0 - 1 .. x0 + 128, C channels, 2C-byte
+// rows) in the swizzled K-major layout whose span is the row (32/64/128 B) —
+// and starts the A operand of output row r, tap (dy, dx) at voxel row
+// (r + dy) * 130 + dx of it.  The swizzle is a function of the shared-memory
+// address bits (the box starts 1024-byte aligned), so a descriptor may start
+// at any row: no copy per tap.  Each output row has its own TMEM
+// accumulator; R rows need (R + 2) / (3 R) of the input rows that one row
+// per tile would load.  When the layer's weights fit (<= 64 KB) they are
+// loaded once per CTA and stay in shared memory; otherwise each stage also
+// carries its nine weight blocks.
 //
 // The kernel is persistent and warp-specialised: warp 0 issues the TMA loads
 // of tile after tile into a ring of stages, warp 1 issues the MMAs into one
 // of two TMEM accumulators, and warps 2-5 drain the other accumulator
 // (tcgen05.ld, bias/ReLU, stores), so a tile's epilogue overlaps the next
 // tile's loads and MMAs.
-template <int COUT, int CMAX, bool RES>
-struct ConvDxCfg {
-    static constexpr int kRows = kCvM + 2;
-    static constexpr int kPlane = kRows * 16;                                    // one dy row of 8 channels
-    static constexpr int kChunk = ((3 * kPlane + 127) / 128) * 128;              // three dy rows
-    static constexpr int kABytes = (((CMAX / 8) * kChunk + 1023) / 1024) * 1024;
-    static constexpr int kBTap = COUT * CMAX * 2;                                // one tap's weight block
-    static constexpr int kStage = kABytes + (RES ? 0 : ((9 * kBTap + 1023) / 1024) * 1024);
-    static constexpr int kBudget = 49152;
-    static constexpr int kStages = (kBudget / kStage) < 2 ? 2 : ((kBudget / kStage) > 6 ? 6 : kBudget / kStage);
-    static constexpr int kAccCols = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);   // one accumulator
-    static constexpr int kTmemCols = 2 * kAccCols;
-    static constexpr int kWMax = 65536;                                          // resident weights, at most
-    static constexpr int kSmemFixed = kStages * kStage + 256 + 1024;
+// Sizes of the tap-reuse kernel for (Cout, widest input segment, resident
+// weights), shared by the kernel's template and the host's routing.
+struct DxSizes {
+    int rows;        // output rows per tile (R)
+    int abytes;      // input bytes of one stage: R + 2 rows of 130 voxels
+    int btap;        // one tap's weight block
+    int stage;       // bytes of one stage (input, and nine weight blocks unless resident)
+    int stages;
+    int acc_cols;    // TMEM columns of one output row's accumulator
+    int tmem_cols;   // two tiles' accumulators
+    int fixed;       // dynamic shared memory besides the resident weights
 };
-constexpr int kDxThreads = 192;   // producer warp, MMA warp, 4 epilogue warps
+constexpr int kDxWMax = 65536;              // resident weights, at most
+constexpr int kDxBudget = 98304;            // stage ring target
+constexpr int kDxThreads = 192;             // producer warp, MMA warp, 4 epilogue warps
 constexpr int kDxSmemLimit = 227 * 1024;
 
-// Host: whether the tap-reuse kernel's shared memory fits for this shape (the
-// same sizes as ConvDxCfg, with the resident-weight choice of launch_conv_dx).
-static bool dx_fits(int cout, int cmax, int nseg) {
-    const int chunk = ((3 * (kCvM + 2) * 16 + 127) / 128) * 128;
-    const int abytes = (((cmax / 8) * chunk + 1023) / 1024) * 1024;
+__host__ __device__ constexpr DxSizes dx_sizes(int cout, int cmax, bool res) {
+    const int rows = cmax == 64 ? (cout <= 64 ? 2 : 1) : (cout <= 64 ? 4 : 2);
+    const int abytes = (((rows + 2) * (kCvM + 2) * cmax * 2 + 1023) / 1024) * 1024;
     const int btap = cout * cmax * 2;
-    const bool res = nseg * 27 * btap <= 65536;
     const int stage = abytes + (res ? 0 : ((9 * btap + 1023) / 1024) * 1024);
-    int stages = 49152 / stage;
-    stages = stages < 2 ? 2 : (stages > 6 ? 6 : stages);
-    return (res ? 65536 : 0) + stages * stage + 256 + 1024 <= kDxSmemLimit;
+    const int fit = kDxBudget / stage;
+    const int stages = fit < 2 ? 2 : (fit > 6 ? 6 : fit);
+    const int acc = cout <= 32 ? 32 : (cout <= 64 ? 64 : 128);
+    return DxSizes{rows, abytes, btap, stage, stages, acc, 2 * rows * acc, stages * stage + 256 + 1024};
+}
+
+template <int COUT, int CMAX, bool RES>
+struct ConvDxCfg {
+    static constexpr DxSizes kS = dx_sizes(COUT, CMAX, RES);
+    static constexpr int kR = kS.rows;
+    static constexpr int kABytes = kS.abytes;
+    static constexpr int kBTap = kS.btap;
+    static constexpr int kStage = kS.stage;
+    static constexpr int kStages = kS.stages;
+    static constexpr int kAccCols = kS.acc_cols;
+    static constexpr int kTmemCols = kS.tmem_cols;
+    static constexpr int kWMax = kDxWMax;
+    static constexpr int kSmemFixed = kS.fixed;
+    static_assert(kTmemCols <= 512, "conv3d_tc_dx_kernel: accumulators above the TMEM of one SM");
+};
+
+// Host: whether the tap-reuse kernel fits for this shape (resident weights
+// when they fit kDxWMax, as launch_conv_dx decides), and its rows per tile.
+static bool dx_fits(int cout, int cmax, int nseg, int *rows) {
+    const bool res = nseg * 27 * cout * cmax * 2 <= kDxWMax;
+    const DxSizes z = dx_sizes(cout, cmax, res);
+    *rows = z.rows;
+    return (res ? kDxWMax : 0) + z.fixed <= kDxSmemLimit;
 }
 
 template <int COUT, int CMAX, int EPI, bool RES>
@@ -240,8 +268,9 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
     volatile int *failed = reinterpret_cast<volatile int *>(tslot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tiles_x = g.W / kCvM;
-    const int ntiles = g.N * g.D * g.H * tiles_x;
+    constexpr int R = Cfg::kR;
+    const int tiles_x = g.W / kCvM, tiles_y = (g.H + R - 1) / R;
+    const int ntiles = g.N * g.D * tiles_y * tiles_x;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < Cfg::kStages; ++s) {
@@ -279,8 +308,8 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                 int t = tile;
                 const int x0 = (t % tiles_x) * kCvM;
                 t /= tiles_x;
-                const int hh = t % g.H;
-                t /= g.H;
+                const int y0 = (t % tiles_y) * R;
+                t /= tiles_y;
                 const int d = t % g.D, n = t / g.D;
                 for (int k = 0; k < steps_per_tile; ++k, ++i) {
                     const int s = i % Cfg::kStages;
@@ -292,11 +321,9 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                     const int c = seg ? g.c1 : g.c0;
                     uint8_t *A = base + s * Cfg::kStage;
                     uint8_t *B = A + Cfg::kABytes;
-                    mbar_arrive_expect_tx(&full[s], (uint32_t)((c / 8) * 3 * Cfg::kPlane +
+                    mbar_arrive_expect_tx(&full[s], (uint32_t)((R + 2) * (kCvM + 2) * c * 2 +
                                                                (RES ? 0 : 9 * COUT * c * 2)));
-                    for (int ch = 0; ch < c / 8; ++ch)
-                        tma_load_5d(A + ch * Cfg::kChunk, seg ? &ta1 : &ta0, ch * 8, x0 - 1, hh - 1, d + dzi - 1, n,
-                                    &full[s]);
+                    tma_load_5d(A, seg ? &ta1 : &ta0, 0, x0 - 1, y0 - 1, d + dzi - 1, n, &full[s]);
                     if (!RES)
                         for (int q = 0; q < 9; ++q)
                             tma_load_2d(B + q * Cfg::kBTap, seg ? &tb1 : &tb0, 0, (dzi * 9 + q) * COUT, &full[s]);
@@ -317,7 +344,7 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                     break;
                 }
                 tc_fence_after();
-                const uint32_t dacc = tmem + (uint32_t)(b * Cfg::kAccCols);
+                const uint32_t dacc = tmem + (uint32_t)(b * R * Cfg::kAccCols);
                 for (int k = 0; k < steps_per_tile; ++k, ++i) {
                     const int s = i % Cfg::kStages;
                     if (!mbar_wait(&full[s], (i / Cfg::kStages) & 1, status)) {
@@ -332,13 +359,16 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                         const uint32_t dy = q / 3u, dx = q % 3u;
                         const uint32_t bt = RES ? w_addr + (uint32_t)(seg * 27 + dzi * 9) * Cfg::kBTap + q * Cfg::kBTap
                                                 : b_addr + q * Cfg::kBTap;
-                        for (uint32_t kk = 0; kk < c / 16; ++kk)
-                            umma_bf16(dacc,
-                                      umma_smem_desc_interleaved(a_addr + dy * Cfg::kPlane + 16u * dx +
-                                                                     2u * kk * Cfg::kChunk,
-                                                                 Cfg::kChunk, 128u),
-                                      umma_smem_desc(bt + 32u * kk, c * 2u), idesc,
-                                      (k > 0 || q > 0 || kk > 0) ? 1u : 0u);
+                        for (uint32_t kk = 0; kk < c / 16; ++kk) {
+                            const uint64_t bd = umma_smem_desc(bt + 32u * kk, c * 2u);
+#pragma unroll
+                            for (uint32_t r = 0; r < (uint32_t)R; ++r) {
+                                const uint64_t ad = umma_smem_desc(
+                                    a_addr + ((r + dy) * (uint32_t)(kCvM + 2) + dx) * (c * 2u) + 32u * kk, c * 2u);
+                                umma_bf16(dacc + r * (uint32_t)Cfg::kAccCols, ad, bd, idesc,
+                                          (k > 0 || q > 0 || kk > 0) ? 1u : 0u);
+                            }
+                        }
                     }
                     umma_commit(&empty[s]);
                 }
@@ -360,11 +390,13 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
             int t = tile;
             const int x0 = (t % tiles_x) * kCvM;
             t /= tiles_x;
-            const int hh = t % g.H;
-            t /= g.H;
+            const int y0 = (t % tiles_y) * R;
+            t /= tiles_y;
             const int d = t % g.D, n = t / g.D;
-            const long long vox = (((long long)n * g.D + d) * g.H + hh) * g.W + x0 + row;
-            const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * Cfg::kAccCols);
+            const int rows = g.H - y0 < R ? g.H - y0 : R;        // rows of this tile inside the volume
+            for (int r = 0; r < rows; ++r) {
+            const long long vox = (((long long)n * g.D + d) * g.H + y0 + r) * g.W + x0 + row;
+            const uint32_t tbase = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((b * R + r) * Cfg::kAccCols);
 #pragma unroll
             for (int cb = 0; cb < COUT; cb += 16) {
                 float v[16];
@@ -384,6 +416,7 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                     for (int q = 0; q < 4; ++q)
                         o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
                 }
+            }
             }
             tc_fence_before();
             mbar_arrive(&acc_empty[b]);
@@ -732,7 +765,9 @@ template <int COUT, int CMAX, int EPI, bool RES>
 static int launch_conv_dx_res(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
                               const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
     using Cfg = ConvDxCfg<COUT, CMAX, RES>;
-    const int wres = RES ? g.nseg * 27 * Cfg::kBTap : 0;
+    // Resident weights, rounded up so that the stage ring starts 1024-byte
+    // aligned (the 128-byte swizzle's repeat).
+    const int wres = RES ? (g.nseg * 27 * Cfg::kBTap + 1023) / 1024 * 1024 : 0;
     const int smem = wres + Cfg::kSmemFixed;
     // Largest dynamic shared memory this instantiation can ask for; shapes
     // that would not fit never get here (ctgb_unet_conv3d routes them to
@@ -750,7 +785,7 @@ static int launch_conv_dx_res(const CUtensorMap &a0, const CUtensorMap &a1, cons
     }
     int *status = ctgb_status_ptr();
     if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
-    const long long tiles = (long long)g.N * g.D * g.H * (g.W / kCvM);
+    const long long tiles = (long long)g.N * g.D * ((g.H + Cfg::kR - 1) / Cfg::kR) * (g.W / kCvM);
     if (tiles > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "conv3d: too many tiles");
     // Persistent grid: as many CTAs as fit on the GPU at once (shared memory,
     // TMEM and thread bound), never more than the tiles.
@@ -804,14 +839,15 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     const int r = 128 / wb;
     if (h % r) return set_error(CTGB_ERR_ARG, "ctgb_unet_conv3d: H must be a multiple of %d for W = %d", r, w);
     ConvGeom g{n, d, h, w, wb, r, c0, c1, c1 ? 2 : 1};
-    // Rows of 128 voxels take the tap reuse kernel: input boxes of 8 channels
-    // x 130 voxels x 3 rows (unswizzled), weight boxes as before.
-    const bool dxr = (w % kCvM) == 0 && dx_fits(cout, c0 > c1 ? c0 : c1, c1 ? 2 : 1);
+    // Rows of 128 voxels take the tap reuse kernel: input boxes of C channels
+    // x 130 voxels x (R + 2) rows, weight boxes as before.
+    int dx_r = 1;
+    const bool dxr = (w % kCvM) == 0 && dx_fits(cout, c0 > c1 ? c0 : c1, c1 ? 2 : 1, &dx_r);
     CUtensorMap ta0, ta1, tb0, tb1;
     {
         const uint64_t dims[5] = {(uint64_t)c0, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c0, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
-                                 dxr ? 3u : (uint32_t)r, 1u, 1u};
+        const uint32_t box[5] = {(uint32_t)c0, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
+                                 dxr ? (uint32_t)(dx_r + 2) : (uint32_t)r, 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c0, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c0, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta0, x0, 5, dims, box) || !ctgb_make_tmap_bf16(&tb0, w0, 2, wd, wbx))
@@ -819,8 +855,8 @@ extern "C" int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int3
     }
     if (c1) {
         const uint64_t dims[5] = {(uint64_t)c1, (uint64_t)w, (uint64_t)h, (uint64_t)d, (uint64_t)n};
-        const uint32_t box[5] = {dxr ? 8u : (uint32_t)c1, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
-                                 dxr ? 3u : (uint32_t)r, 1u, 1u};
+        const uint32_t box[5] = {(uint32_t)c1, dxr ? (uint32_t)(kCvM + 2) : (uint32_t)wb,
+                                 dxr ? (uint32_t)(dx_r + 2) : (uint32_t)r, 1u, 1u};
         const uint64_t wd[2] = {(uint64_t)c1, (uint64_t)(27 * cout)};
         const uint32_t wbx[2] = {(uint32_t)c1, (uint32_t)cout};
         if (!ctgb_make_tmap_bf16(&ta1, x1, 5, dims, box) || !ctgb_make_tmap_bf16(&tb1, w1, 2, wd, wbx))
