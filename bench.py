@@ -548,7 +548,9 @@ def run_asd256(args):
 def run_asd256_learned(args):
     """Learned proximal step at 256^3, 60 views, 512x384 detector: (1) 2,000
     (pre-TV, post-TV) crop pairs (32x32x64) from plain ASD-POCS on 8 training
-    phantoms (25 iterations x 10 crops each); (2) training of the 3-D U-Net
+    phantoms from a zero start (25 pairs x 10 crops each; with --ahead K the
+    volume before the TV step of iteration k is paired with the volume after
+    the TV step of iteration k + K); (2) training of the 3-D U-Net
     (Adam, batch 8); (3) plain and learned ASD-POCS on a held-out phantom,
     20 iterations each, the learned step judged against the plain TV step on
     every iteration (data residual within 1 %).  Both runs start from a zero
@@ -568,7 +570,11 @@ def run_asd256_learned(args):
     asd = dict(alpha=0.002, ng=20, na=5)
     t0 = time.perf_counter()
     train_ph = [phantoms.random_ellipsoids((256, 256, 256), n=30, seed=100 + i, device=dev) * 0.02 for i in range(8)]
-    pairs = learned.tv_pairs(P, train_ph, niter=25, crops=10, size=(32, 32, 64), seed=0, **asd)
+    zero = torch.zeros((256, 256, 256), device=dev)
+    # 25 + K iterations per phantom from a zero start, 10 crops per pair
+    # (pre-TV at k, post-TV at k + K): 8 x 25 x 10 = 2,000 pairs.
+    pairs = learned.tv_pairs(P, train_ph, niter=25 + args.ahead, crops=10, size=(32, 32, 64), seed=0,
+                             ahead=args.ahead, x0=zero, **asd)
     del train_ph
     torch.cuda.synchronize()
     t_pairs = time.perf_counter() - t0
@@ -577,11 +583,11 @@ def run_asd256_learned(args):
     losses = learned.train(net, pairs, steps=args.train_steps, batch=8, size=(32, 32, 64), lr=1e-3, seed=0)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    n_pairs = len(pairs)
     del pairs
     ph = phantoms.random_ellipsoids((256, 256, 256), n=30, seed=5, device=dev) * 0.02
     proj0 = P.forward(ph)
     niter = 20
-    zero = torch.zeros_like(ph)
     iterative.asd_pocs(P, proj0, niter=1, norms=norms, x0=zero, **asd)          # warm
     t_plain = []
     _, rmse_plain, _ = iterative.asd_pocs(P, proj0, niter=niter, norms=norms, phantom=ph, times=t_plain, x0=zero,
@@ -614,7 +620,8 @@ def run_asd256_learned(args):
             "higher_is_better": False, "dtype": "bf16 U-Net / f32 projectors",
             "data": "synthetic (random ellipsoids, 8 training phantoms + 1 held out)",
             "config": {"workload": "asd_pocs_learned_256cube_60views_det512x384", "alpha": 0.002, "ng": 20,
-                       "na": 5, "iterations": niter, "pairs": 2000, "train_steps": args.train_steps},
+                       "na": 5, "iterations": niter, "pairs": n_pairs, "train_steps": args.train_steps,
+                       "pair_ahead": args.ahead},
             "rmse_plain": rmse_plain, "rmse_learned": rmse_learn, "plain_s": t_plain[-1],
             "learned_s_per_iteration": t_learn[-1] / niter, "plain_s_per_iteration": t_plain[-1] / niter,
             "learned_reaches_target_at_iteration": reach, "accepted": prox.accepted, "rejected": prox.rejected,
@@ -662,6 +669,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-matched", action="store_true")
     ap.add_argument("--train-steps", type=int, default=1500, help="U-Net training steps (asd256_learned)")
+    ap.add_argument("--ahead", type=int, default=0,
+                    help="training pairs (pre-TV at k, post-TV at k + AHEAD) (asd256_learned)")
     ap.add_argument("--workload", default="dd512", choices=["dd512"] + sorted(WORKLOADS),
                     help="dd512 (default) is the headline DD pair; the others time the remaining configurations")
     args = ap.parse_args()

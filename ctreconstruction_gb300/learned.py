@@ -368,17 +368,25 @@ class LearnedProx:
         return cand
 
 
-def tv_pairs(projector, phantom_list, niter, crops, size, seed=0, **asd_kwargs):
+def tv_pairs(projector, phantom_list, niter, crops, size, seed=0, ahead=0, **asd_kwargs):
     """(pre-TV, post-TV) training pairs from ASD-POCS itself: for each
     phantom, project it, run `niter` ASD-POCS iterations and keep `crops`
     random crops of `size` from the volume before and after every TV step.
-    Returns a list of (pre, post) device tensors."""
+
+    ahead = K > 0 pairs the volume before the TV step of iteration k with
+    the volume after the TV step of iteration k + K (same crop), for
+    k = 0 .. niter - 1 - K: a network fitted to these pairs steps K
+    iterations along the plain run's trajectory per call.  Returns a list of
+    (pre, post) device tensors."""
     from . import iterative
     gen = torch.Generator().manual_seed(seed)
     d, h, w = size
+    ahead = int(ahead)
+    if ahead < 0 or ahead >= niter:
+        raise ValueError("ahead must be in [0, niter)")
     pairs = []
 
-    def keep(pre, post):
+    def crop_pairs(pre, post):
         nz, ny, nx = pre.shape
         for _ in range(crops):
             z = int(torch.randint(nz - d + 1, (1,), generator=gen))
@@ -389,5 +397,14 @@ def tv_pairs(projector, phantom_list, niter, crops, size, seed=0, **asd_kwargs):
     norms = iterative.normalisers(projector)
     for ph in phantom_list:
         proj0 = projector.forward(ph)
-        iterative.asd_pocs(projector, proj0, niter=niter, norms=norms, on_tv=keep, **asd_kwargs)
+        if ahead == 0:
+            iterative.asd_pocs(projector, proj0, niter=niter, norms=norms, on_tv=crop_pairs, **asd_kwargs)
+            continue
+        pres, posts = [], []
+        iterative.asd_pocs(projector, proj0, niter=niter, norms=norms,
+                           on_tv=lambda pre, post: (pres.append(pre.clone()), posts.append(post.clone())),
+                           **asd_kwargs)
+        for k in range(niter - ahead):
+            crop_pairs(pres[k], posts[k + ahead])
+        del pres, posts
     return pairs

@@ -107,6 +107,67 @@ class Reconstruction:
             return out
         return _host(t)
 
+    # -- pipelined host transfers ---------------------------------------------------
+    # Pinned host tensors go through the projectors in chunks of views: each
+    # chunk's device-to-host (forward) or host-to-device (backward) copy runs
+    # on a second stream while the kernels of the neighbouring chunk run, so
+    # the copies hide behind the projector instead of adding to it.
+    CHUNKS = 8
+
+    def _chunks(self, n):
+        k = max(1, min(self.CHUNKS, n))
+        step = (n + k - 1) // k
+        return [(a, min(step, n - a)) for a in range(0, n, step)]
+
+    def _device_buffer(self, key, shape):
+        cache = self.__dict__.setdefault("_dev", {})
+        buf = cache.get(key)
+        if buf is None or tuple(buf.shape) != tuple(shape):
+            buf = torch.empty(shape, dtype=torch.float32, device=self.projector.device)
+            cache[key] = buf
+        return buf
+
+    def _streams(self):
+        dev = self.projector.device
+        if self.__dict__.get("_copy_stream") is None:
+            self._copy_stream = torch.cuda.Stream(device=dev)
+        return torch.cuda.current_stream(dev), self._copy_stream
+
+    def _forward_pinned(self, src):
+        P = self.projector
+        compute, copy = self._streams()
+        vol = _to_device(src, P.device)
+        xzy = P.transpose(vol)
+        shape = P.proj_shape()
+        dev = self._device_buffer("proj", shape)
+        out = _pinned_like(self.__dict__.setdefault("_pinned", {}), "proj", dev)
+        for v0, n in self._chunks(shape[0]):
+            P.forward(vol, out=dev[v0:v0 + n], view0=v0, nviews=n, transposed=xzy)
+            done = torch.cuda.Event()
+            done.record(compute)
+            copy.wait_event(done)
+            with torch.cuda.stream(copy):
+                out[v0:v0 + n].copy_(dev[v0:v0 + n], non_blocking=True)
+        copy.synchronize()
+        return out
+
+    def _backward_pinned(self, src):
+        P = self.projector
+        compute, copy = self._streams()
+        shape = P.proj_shape()
+        if tuple(src.shape) != tuple(shape):
+            raise ValueError("proj must have shape %s, got %s" % (shape, tuple(src.shape)))
+        q = self._device_buffer("proj_in", shape)
+        vol = torch.empty(P.volume_shape, dtype=torch.float32, device=P.device)
+        for i, (v0, n) in enumerate(self._chunks(shape[0])):
+            with torch.cuda.stream(copy):
+                q[v0:v0 + n].copy_(src[v0:v0 + n], non_blocking=True)
+            landed = torch.cuda.Event()
+            landed.record(copy)
+            compute.wait_event(landed)
+            P.backproject_fdk(q[v0:v0 + n], out=vol, view0=v0, nviews=n, accumulate=i > 0)
+        return self._to_host(vol, src, "image")
+
     # -- projectors ----------------------------------------------------------------
     def forward(self):
         """self.proj = forward projection of self.image: DD (distance_forward)
@@ -116,6 +177,9 @@ class Reconstruction:
             return
         src = self.image
         host = _on_host(src)
+        if host and self.Method == 'Distance' and isinstance(src, torch.Tensor) and src.is_pinned():
+            self.proj = self._forward_pinned(src)
+            return
         vol = _to_device(src, self.projector.device)
         proj = self.projector.forward(vol) if self.Method == 'Distance' else self.projector.ray_forward(vol)
         self.proj = self._to_host(proj, src, "proj") if host else proj
@@ -129,6 +193,9 @@ class Reconstruction:
             return
         src = self.proj
         host = _on_host(src)
+        if host and self.Method == 'Distance' and isinstance(src, torch.Tensor) and src.is_pinned():
+            self.image = self._backward_pinned(src)
+            return
         q = _to_device(src, self.projector.device)
         if self.Method == 'Distance':
             vol = self.projector.backproject_fdk(q)
