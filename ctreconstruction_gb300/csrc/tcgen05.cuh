@@ -34,6 +34,13 @@ __device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, uint32_t row_
     return d;
 }
 
+// The same descriptor with its start address moved by delta16 * 16 bytes.
+// The start field is the low 14 bits and shared memory is below 256 KB, so
+// the addition never carries out of the field: a 32-bit add on the low word.
+__device__ __forceinline__ uint64_t desc_advance(uint64_t d, uint32_t delta16) {
+    return (d & 0xFFFFFFFF00000000ull) | (uint64_t)((uint32_t)d + delta16);
+}
+
 // Descriptor of a K-major operand in the unswizzled (interleaved) layout:
 // 8 x 16-byte core matrices whose 8 rows are 16 bytes apart, core matrices
 // adjacent in K `lbo` bytes apart and 8-row groups `sbo` bytes apart; the

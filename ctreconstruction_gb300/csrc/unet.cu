@@ -175,7 +175,7 @@ conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant_
 // ---- tap reuse for rows of 128 voxels ------------------------------------------
 //
 // When W is a multiple of 128 a tile is R runs of 128 voxels along x, in R
-// consecutive rows y0 .. y0 + R - 1 (R = 4, 2 or 1 by the layer's channel
+// consecutive rows y0 .. y0 + R - 1 (R = 1 or 2 by the layer's channel
 // counts; rows past H are computed from zero fill and not stored).  For one
 // dz plane, the 9 R (row, dy, dx) products read R + 2 input rows
 // (y0 - 1 .. y0 + R), each shifted by one voxel per dx.
@@ -187,7 +187,7 @@ conv3d_tc_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant_
 // address bits (the box starts 1024-byte aligned), so a descriptor may start
 // at any row: no copy per tap.  Each output row has its own TMEM
 // accumulator; R rows need (R + 2) / (3 R) of the input rows that one row
-// per tile would load.  When the layer's weights fit (<= 64 KB) they are
+// per tile would load.  When the layer's weights fit (<= 16 KB) they are
 // loaded once per CTA and stay in shared memory; otherwise each stage also
 // carries its nine weight blocks.
 //
@@ -208,13 +208,32 @@ struct DxSizes {
     int tmem_cols;   // two tiles' accumulators
     int fixed;       // dynamic shared memory besides the resident weights
 };
-constexpr int kDxWMax = 65536;              // resident weights, at most
-constexpr int kDxBudget = 98304;            // stage ring target
+// Occupancy decides this kernel's speed: each CTA has one MMA-issuing
+// thread, and the Cout = 16 layers ran fastest with four CTAs per SM.  At
+// 256^3 (one U-Net forward): resident weights only up to 16 KB, two output
+// rows per tile for 16- and 32-channel inputs and a 48 KB stage ring gave
+// 6.26 ms; four rows, 64 KB resident weights and a 96 KB ring 7.27 ms (one
+// or two CTAs per SM); one row per tile 6.8-6.9 ms; no resident weights
+// 7.61 ms.
+#ifndef CTGB_DX_WMAX
+#define CTGB_DX_WMAX 16384
+#endif
+#ifndef CTGB_DX_R32
+#define CTGB_DX_R32 2
+#endif
+#ifndef CTGB_DX_R16
+#define CTGB_DX_R16 2
+#endif
+constexpr int kDxWMax = CTGB_DX_WMAX;       // resident weights, at most
+#ifndef CTGB_DX_BUDGET
+#define CTGB_DX_BUDGET 49152
+#endif
+constexpr int kDxBudget = CTGB_DX_BUDGET;   // stage ring target
 constexpr int kDxThreads = 192;             // producer warp, MMA warp, 4 epilogue warps
 constexpr int kDxSmemLimit = 227 * 1024;
 
 __host__ __device__ constexpr DxSizes dx_sizes(int cout, int cmax, bool res) {
-    const int rows = cmax == 64 ? (cout <= 64 ? 2 : 1) : (cout <= 64 ? 4 : 2);
+    const int rows = cmax == 64 ? (cout <= 64 ? 2 : 1) : (cout <= 64 ? (cmax == 32 ? CTGB_DX_R32 : CTGB_DX_R16) : 2);
     const int abytes = (((rows + 2) * (kCvM + 2) * cmax * 2 + 1023) / 1024) * 1024;
     const int btap = cout * cmax * 2;
     const int stage = abytes + (res ? 0 : ((9 * btap + 1023) / 1024) * 1024);
@@ -353,21 +372,26 @@ conv3d_tc_dx_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_consta
                     }
                     tc_fence_after();
                     const int dzi = k / g.nseg, seg = k - dzi * g.nseg;
-                    const uint32_t c = (uint32_t)(seg ? g.c1 : g.c0);
+                    const uint32_t c = (uint32_t)(seg ? g.c1 : g.c0), rowb = c * 2u, nk = c / 16u;
                     const uint32_t a_addr = smem_addr(base + s * Cfg::kStage), b_addr = a_addr + Cfg::kABytes;
+                    // Base descriptors of the stage's input rows and of its (or
+                    // the resident) weight blocks; every product's descriptor is
+                    // one of these plus a start offset in 16-byte units.
+                    const uint64_t a0 = umma_smem_desc(a_addr, rowb);
+                    const uint64_t b0 =
+                        umma_smem_desc(RES ? w_addr + (uint32_t)(seg * 27 + dzi * 9) * Cfg::kBTap : b_addr, rowb);
+                    const uint32_t row16 = (uint32_t)(kCvM + 2) * (rowb >> 4), vox16 = rowb >> 4;
+#pragma unroll
                     for (uint32_t q = 0; q < 9; ++q) {
                         const uint32_t dy = q / 3u, dx = q % 3u;
-                        const uint32_t bt = RES ? w_addr + (uint32_t)(seg * 27 + dzi * 9) * Cfg::kBTap + q * Cfg::kBTap
-                                                : b_addr + q * Cfg::kBTap;
-                        for (uint32_t kk = 0; kk < c / 16; ++kk) {
-                            const uint64_t bd = umma_smem_desc(bt + 32u * kk, c * 2u);
+                        for (uint32_t kk = 0; kk < nk; ++kk) {
+                            const uint64_t bd = desc_advance(b0, (q * (uint32_t)Cfg::kBTap >> 4) + 2u * kk);
+                            const uint64_t ab = desc_advance(a0, dy * row16 + dx * vox16 + 2u * kk);
+                            const uint32_t accum = (k > 0 || q > 0 || kk > 0) ? 1u : 0u;
 #pragma unroll
-                            for (uint32_t r = 0; r < (uint32_t)R; ++r) {
-                                const uint64_t ad = umma_smem_desc(
-                                    a_addr + ((r + dy) * (uint32_t)(kCvM + 2) + dx) * (c * 2u) + 32u * kk, c * 2u);
-                                umma_bf16(dacc + r * (uint32_t)Cfg::kAccCols, ad, bd, idesc,
-                                          (k > 0 || q > 0 || kk > 0) ? 1u : 0u);
-                            }
+                            for (uint32_t r = 0; r < (uint32_t)R; ++r)
+                                umma_bf16(dacc + r * (uint32_t)Cfg::kAccCols, desc_advance(ab, r * row16), bd, idesc,
+                                          accum);
                         }
                     }
                     umma_commit(&empty[s]);
@@ -809,7 +833,7 @@ static int launch_conv_dx_res(const CUtensorMap &a0, const CUtensorMap &a1, cons
 template <int COUT, int CMAX, int EPI>
 static int launch_conv_dx(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0,
                           const CUtensorMap &b1, const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
-    // Weights resident when they fit the 64 KB budget.
+    // Weights resident when they fit kDxWMax.
     const long long wres = (long long)g.nseg * 27 * ConvDxCfg<COUT, CMAX, true>::kBTap;
     if (wres <= ConvDxCfg<COUT, CMAX, true>::kWMax)
         return launch_conv_dx_res<COUT, CMAX, EPI, true>(a0, a1, b0, b1, g, bias, out, st);
