@@ -630,6 +630,73 @@ def run_asd256_learned(args):
             "unet_tflops": flops / (unet_ms / 1e3) / 1e12, "tv20_ms_256cube": tv_ms}
 
 
+def run_rows(args):
+    """The hot path's other rows at 256^3 (0.5 mm), 360 views, 512x384
+    detector (0.75 mm), SAD 1000 mm, SDD 1500 mm, 30 seeded random
+    ellipsoids; each timed with CUDA events, inputs and outputs on the
+    device, in Gvoxel*views/s: the DD pair (forward + FDK-weighted
+    backprojection) on a flat detector, on a curved (equiangular
+    cylindrical) detector and on a helical orbit (pitch 0.5); the Siddon
+    ray-driven pair (forward + transpose); the voxel-driven ConeBeamGPU
+    backprojection (360 views onto 256^3).  `value` is the curved DD pair."""
+    import ctypes
+    import torch
+    from ctreconstruction_gb300 import Projector, _lib, phantoms
+    from ctreconstruction_gb300.projector import _ptr, _stream
+    from ctreconstruction_gb300.standalone import _cparams
+    dev = torch.device("cuda", torch.cuda.current_device())
+    n, nviews, nu, nv = (args.small or 256), 360, 512, 384
+    base = scan_params(n, nviews, nu, nv)
+    ph = phantoms.random_ellipsoids((n, n, n), n=30, seed=1, device=dev) * 0.02
+    vv = n ** 3 * nviews
+    detail = {}
+
+    def rate(ms):
+        return {"ms": ms, "Gvoxel_views_per_s": vv / (ms / 1e3) / 1e9}
+
+    for name, extra in (("dd_pair_curved", {'DetectorShape': 'Curved'}), ("dd_pair_helical", {'Pitch': 0.5}),
+                        ("dd_pair_flat", {})):
+        P = Projector(dict(base, **extra), device=dev)
+        proj = torch.empty(P.proj_shape(), device=dev)
+        vol = torch.empty_like(ph)
+
+        def pair(P=P, proj=proj, vol=vol):
+            P.forward(ph, out=proj)
+            P.backproject_fdk(proj, out=vol)
+
+        detail[name] = rate(_timed(pair, args.steps, args.warmup))
+    P = Projector(dict(base, Method='Ray'), device=dev)
+    proj = torch.empty(P.proj_shape(), device=dev)
+    vol = torch.empty_like(ph)
+
+    def ray_pair():
+        P.ray_forward(ph, out=proj)
+        P.ray_backproject(proj, out=vol)
+
+    detail["siddon_pair"] = rate(_timed(ray_pair, args.steps, args.warmup))
+    c = _cparams({'SourceToAxis': 1000.0, 'SourceToDetector': 1500.0, 'DetectorPixelWidth': 0.75,
+                  'DetectorPixelHeight': 0.75, 'DetectorWidth': nu, 'DetectorHeight': nv, 'NumberOfViews': nviews,
+                  'AngleCoverage': 2 * np.pi, 'ReconX': n, 'ReconY': n, 'ReconZ': n})
+    nb = ctypes.c_size_t(0)
+    _lib.call("ctgb_conebeam_table_bytes", ctypes.byref(c), ctypes.byref(nb))
+    host = np.zeros(nb.value // 4, dtype=np.float32)
+    _lib.call("ctgb_conebeam_table_build", ctypes.byref(c), host.ctypes.data_as(ctypes.c_void_p), nb.value)
+    table = torch.from_numpy(host).to(dev)
+    q = torch.rand((nviews, nv, nu), device=dev, generator=torch.Generator(device=dev).manual_seed(2))
+    recon = torch.empty((n, n, n), device=dev)
+
+    def cone_bp():
+        _lib.call("ctgb_conebeam_backproject", ctypes.byref(c), _ptr(table), _ptr(q), _ptr(recon), 0, nviews, 0,
+                  _stream())
+
+    detail["conebeam_fdk_backprojection"] = rate(_timed(cone_bp, args.steps, args.warmup))
+    return {"metric": "hot-path rows throughput (curved DD pair; detail: helical, flat, Siddon, voxel-driven FDK)",
+            "value": detail["dd_pair_curved"]["Gvoxel_views_per_s"], "unit": UNIT,
+            "ms_per_step": detail["dd_pair_curved"]["ms"], "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (30 seeded random ellipsoids; uniform random projections for the voxel-driven BP)",
+            "config": {"workload": "rows_%dcube_%dviews_det%dx%d" % (n, nviews, nu, nv)}, "detail": detail}
+
+
 def run_unet(args):
     """Forward pass of the learned proximal step's 3-D U-Net on one 256^3
     volume (--small N: N^3), bf16 tcgen05 convolutions; reports ms per pass
@@ -655,7 +722,7 @@ def run_unet(args):
                          "peak_source": kind, "flops_per_pass": flops}}
 
 
-WORKLOADS = {"unet": run_unet, "fdk128": run_fdk128, "fan_batch": run_fan_batch, "iter": run_iter, "asd256": run_asd256,
+WORKLOADS = {"rows": run_rows, "unet": run_unet, "fdk128": run_fdk128, "fan_batch": run_fan_batch, "iter": run_iter, "asd256": run_asd256,
              "asd256_learned": run_asd256_learned}
 
 

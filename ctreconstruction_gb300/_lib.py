@@ -65,6 +65,7 @@ SIGNATURES = {
     "ctgb_ray_backproject": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_unet_conv3d": [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp],
     "ctgb_unet_input": [_vp, _vp, _vp, _i32, ctypes.c_int64, _vp],
+    "ctgb_unet_first": [_vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _vp],
     "ctgb_unet_pool2": [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
     "ctgb_unet_up2": [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp],
     "ctgb_unet_relu_grad": [_vp, _i32, _i32, _vp, _vp, ctypes.c_int64, _i32, _vp],

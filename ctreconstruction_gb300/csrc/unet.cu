@@ -471,6 +471,84 @@ __global__ void unet_input_kernel(const float *__restrict__ x, const float *__re
     }
 }
 
+// The first layer on CUDA cores: out = relu(conv(a) + bias) with
+// a = bf16(x / scale[sample]) the network's single real input channel — the
+// same values as ctgb_unet_input followed by the 16-channel tensor-core
+// convolution, whose channels 1-15 are zeros.  A block owns 256 x 8 output
+// voxels of one z plane: it first stages a for the 3 x 10 x 258 input
+// neighbourhood in shared memory (each value divided and rounded once),
+// then each thread computes two voxels of each of the 8 rows: per tap, the
+// two neighbours and the tap's 16 weights (broadcast float4 reads) feed 32
+// FMAs; bias, ReLU and one 32-byte store per voxel.
+constexpr int kFirstThreads = 128, kFirstX = 256, kFirstRows = 8;
+
+__device__ __forceinline__ void first_store(__nv_bfloat16 *dst, const float (&acc)[16], const float *bs) {
+    uint32_t p[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        p[q] = pack_bf16x2(fmaxf(acc[2 * q] + bs[2 * q], 0.0f), fmaxf(acc[2 * q + 1] + bs[2 * q + 1], 0.0f));
+    uint4 *o = reinterpret_cast<uint4 *>(dst);
+    o[0] = make_uint4(p[0], p[1], p[2], p[3]);
+    o[1] = make_uint4(p[4], p[5], p[6], p[7]);
+}
+
+__global__ void __launch_bounds__(kFirstThreads)
+unet_first_kernel(const float *__restrict__ x, const float *__restrict__ scale, const __nv_bfloat16 *__restrict__ w0,
+                  int cin, const float *__restrict__ bias, __nv_bfloat16 *__restrict__ out, int D, int H, int W) {
+    constexpr int SX = kFirstX + 2, SY = kFirstRows + 2;
+    __shared__ float sa[3][SY][SX];
+    __shared__ float4 ws[27][4];   // tap t, outputs 4q .. 4q + 3
+    __shared__ float bs[16];
+    const int x0 = blockIdx.x * kFirstX, y0 = blockIdx.y * kFirstRows;
+    const int zz = blockIdx.z % D, nn = blockIdx.z / D;
+    const float s = scale[nn];
+    const float *__restrict__ xs = x + (size_t)nn * D * H * W;
+    for (int i = threadIdx.x; i < 27 * 16; i += kFirstThreads)
+        reinterpret_cast<float *>(&ws[0][0])[i] = __bfloat162float(w0[(size_t)i * cin]);
+    if (threadIdx.x < 16) bs[threadIdx.x] = bias[threadIdx.x];
+    for (int i = threadIdx.x; i < 3 * SY * SX; i += kFirstThreads) {
+        const int rx = i % SX, ry = (i / SX) % SY, dz = i / (SX * SY);
+        const int z = zz + dz - 1, y = y0 + ry - 1, xi = x0 + rx - 1;
+        float v = 0.0f;
+        if (z >= 0 && z < D && y >= 0 && y < H && xi >= 0 && xi < W)
+            v = __bfloat162float(__float2bfloat16_rn(__ldg(xs + ((size_t)z * H + y) * W + xi) / s));
+        sa[dz][ry][rx] = v;
+    }
+    __syncthreads();
+    const int t0 = threadIdx.x, t1 = threadIdx.x + kFirstThreads;   // the thread's two voxels in the run
+    const bool ok0 = x0 + t0 < W, ok1 = x0 + t1 < W;
+    for (int r = 0; r < kFirstRows && y0 + r < H; ++r) {
+        float acc0[16], acc1[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc0[c] = acc1[c] = 0.0f;
+        // Taps rolled over (dz, dy): the weights are re-read from shared
+        // memory per row instead of being hoisted into 432 registers.
+#pragma unroll 1
+        for (int tzy = 0; tzy < 9; ++tzy) {
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+            const int t = tzy * 3 + dx, dz = tzy / 3, dy = tzy % 3;
+            const float a0 = sa[dz][r + dy][t0 + dx], a1 = sa[dz][r + dy][t1 + dx];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 wq = ws[t][q];
+                acc0[4 * q] = fmaf(wq.x, a0, acc0[4 * q]);
+                acc0[4 * q + 1] = fmaf(wq.y, a0, acc0[4 * q + 1]);
+                acc0[4 * q + 2] = fmaf(wq.z, a0, acc0[4 * q + 2]);
+                acc0[4 * q + 3] = fmaf(wq.w, a0, acc0[4 * q + 3]);
+                acc1[4 * q] = fmaf(wq.x, a1, acc1[4 * q]);
+                acc1[4 * q + 1] = fmaf(wq.y, a1, acc1[4 * q + 1]);
+                acc1[4 * q + 2] = fmaf(wq.z, a1, acc1[4 * q + 2]);
+                acc1[4 * q + 3] = fmaf(wq.w, a1, acc1[4 * q + 3]);
+            }
+        }
+        }
+        __nv_bfloat16 *row = out + (((size_t)nn * D + zz) * H + y0 + r) * W * 16;
+        if (ok0) first_store(row + (size_t)(x0 + t0) * 16, acc0, bs);
+        if (ok1) first_store(row + (size_t)(x0 + t1) * 16, acc1, bs);
+    }
+}
+
 __device__ __forceinline__ void unpack8(uint4 u, float *f) {
     const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
 #pragma unroll
@@ -929,6 +1007,20 @@ extern "C" int ctgb_unet_input(const float *x, const float *scale, void *out, in
     unet_input_kernel<<<grid_for(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         x, scale, static_cast<__nv_bfloat16 *>(out), vps, total);
     return ew_done("unet_input_kernel");
+}
+
+extern "C" int ctgb_unet_first(const float *x, const float *scale, const void *w0, int32_t cin, const float *bias,
+                               void *out, int32_t n, int32_t d, int32_t h, int32_t w, void *stream) {
+    clear_error();
+    if (!x || !scale || !w0 || !bias || !out) return set_error(CTGB_ERR_ARG, "ctgb_unet_first: NULL argument");
+    if (cin < 1 || n < 1 || d < 1 || h < 1 || w < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_first: bad sizes");
+    if ((long long)n * d > 65535) return set_error(CTGB_ERR_SIZE, "ctgb_unet_first: N * D must be at most 65535");
+    dim3 grid((unsigned)((w + kFirstX - 1) / kFirstX), (unsigned)((h + kFirstRows - 1) / kFirstRows),
+              (unsigned)(n * d));
+    unet_first_kernel<<<grid, kFirstThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        x, scale, static_cast<const __nv_bfloat16 *>(w0), cin, bias, static_cast<__nv_bfloat16 *>(out), d, h, w);
+    return ew_done("unet_first_kernel");
 }
 
 extern "C" int ctgb_unet_pool2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c,

@@ -153,11 +153,17 @@ class UNet3D:
         fw, bw = self._weights(need_bw=keep)
         P = self.params
         L1, L2, L3 = (n, d, h, w), (n, d // 2, h // 2, w // 2), (n, d // 4, h // 4, w // 4)
-        a0 = _bf((n, d, h, w, 16), self.device)
-        _lib.call("ctgb_unet_input", _ptr(x), _ptr(scale), _ptr(a0), n, d * h * w, _stream())
         bias = {k: P[k + ".b"].detach() for k, _, _ in LAYERS}
-        act = {"a0": a0}
-        act["e1a"] = self._conv([(a0, 16)], fw["e1a"], bias["e1a"], 16, L1, 0)
+        act = {}
+        if keep:
+            # the packed input is kept for e1a's weight gradient
+            act["a0"] = _bf((n, d, h, w, 16), self.device)
+            _lib.call("ctgb_unet_input", _ptr(x), _ptr(scale), _ptr(act["a0"]), n, d * h * w, _stream())
+        # e1a has one real input channel: a CUDA-core pass from x itself
+        # instead of 16-channel tensor-core work on mostly zeros.
+        act["e1a"] = _bf((n, d, h, w, 16), self.device)
+        _lib.call("ctgb_unet_first", _ptr(x), _ptr(scale), _ptr(fw["e1a"][0]), 16, _ptr(bias["e1a"]),
+                  _ptr(act["e1a"]), n, d, h, w, _stream())
         act["e1b"] = self._conv([(act["e1a"], 16)], fw["e1b"], bias["e1b"], 16, L1, 0)
         act["p1"] = self._pool(act["e1b"], L1)
         act["e2a"] = self._conv([(act["p1"], 16)], fw["e2a"], bias["e2a"], 32, L2, 0)

@@ -281,6 +281,13 @@ int ctgb_unet_conv3d(const void *x0, int32_t c0, const void *x1, int32_t c1, con
                      int32_t mode, void *stream);
 /* x fp32 [n][vps] -> bf16 [n][vps][16] with channel 0 = x / scale[sample]. */
 int ctgb_unet_input(const float *x, const float *scale, void *out, int32_t n, int64_t vps, void *stream);
+/* The first layer in one pass on CUDA cores: out bf16 [n][d][h][w][16] =
+ * relu(conv(a) + bias) with a = bf16(x / scale[sample]), x fp32 [n][d][h][w]
+ * — ctgb_unet_input followed by ctgb_unet_conv3d (mode 0) on its 16-channel
+ * output, whose channels 1-15 are zero.  w0: the conv's bf16 weight block
+ * [27][16][cin]; only input channel 0 is read.  N * D at most 65535. */
+int ctgb_unet_first(const float *x, const float *scale, const void *w0, int32_t cin, const float *bias, void *out,
+                    int32_t n, int32_t d, int32_t h, int32_t w, void *stream);
 /* 2x2x2 average pooling and nearest 2x upsampling (bf16, c a multiple of 8;
  * d, h, w are the fine dims for pooling and the output dims for upsampling). */
 int ctgb_unet_pool2(const void *in, void *out, int32_t n, int32_t d, int32_t h, int32_t w, int32_t c, void *stream);

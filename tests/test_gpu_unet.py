@@ -75,6 +75,35 @@ def test_conv3d_matches_torch(cuda, c0, c1, cout, dims):
     assert _rel(act.float().cpu(), ref_act.cpu()) < 1e-2           # one bf16 rounding apart at most
 
 
+@pytest.mark.parametrize("dims", [(1, 4, 32, 64), (2, 3, 5, 128), (1, 2, 3, 200)])
+def test_first_layer_matches_input_and_conv(cuda, dims):
+    """ctgb_unet_first (CUDA cores, from x) against ctgb_unet_input followed by
+    the tensor-core conv on the packed 16-channel input: the same bf16
+    products, fp32 sums in another order, so outputs agree to one bf16
+    rounding and almost all are identical."""
+    n, d, h, w = dims
+    gen = torch.Generator(device=cuda).manual_seed(d * h + w)
+    x = torch.randn((n, d, h, w), device=cuda, generator=gen) * 0.02
+    scale = torch.rand(n, device=cuda, generator=gen) * 0.02 + 0.01
+    wt = (torch.randn((27, 16, 16), device=cuda, generator=gen) * 0.3).to(torch.bfloat16).reshape(27 * 16, 16)
+    bias = torch.randn(16, device=cuda, generator=gen) * 0.1
+    got = torch.empty((n, d, h, w, 16), device=cuda, dtype=torch.bfloat16)
+    _lib.call("ctgb_unet_first", _ptr(x), _ptr(scale), _ptr(wt), 16, _ptr(bias), _ptr(got), n, d, h, w, _stream())
+    a0 = torch.empty((n, d, h, w, 16), device=cuda, dtype=torch.bfloat16)
+    _lib.call("ctgb_unet_input", _ptr(x), _ptr(scale), _ptr(a0), n, d * h * w, _stream())
+    torch.cuda.synchronize()
+    want = _torch_conv(a0, wt.reshape(27, 16, 16))
+    want = torch.relu(want + bias).to(torch.bfloat16)
+    assert _rel(got.float().cpu(), want.float().cpu()) < 1e-2
+    assert (got == want).float().mean().item() > 0.98
+    if w % 128 == 0 or w in (16, 32, 64):
+        ref = torch.empty_like(got)
+        _lib.call("ctgb_unet_conv3d", _ptr(a0), 16, None, 0, _ptr(wt), None, _ptr(bias), _ptr(ref), 16, n, d, h, w, 0,
+                  _stream())
+        torch.cuda.synchronize()
+        assert _rel(got.float().cpu(), ref.float().cpu()) < 1e-2
+
+
 def test_conv3d_rejects_bad_shapes(cuda):
     x = torch.zeros((1, 2, 3, 48, 16), device=cuda, dtype=torch.bfloat16)
     wt = torch.zeros((27 * 16, 16), device=cuda, dtype=torch.bfloat16)
