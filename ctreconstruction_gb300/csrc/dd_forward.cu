@@ -184,7 +184,7 @@ struct PatchCells {
 // caller).  No data-dependent branches.
 template <int NT, bool MID, int N>
 __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float *Bj, float A, float tau, float g,
-                                            float *acc) {
+                                            float2 *acc2) {
     float f0a, f0b;
     const float z0a = fmaf(Bj[0], tau, A), z0b = fmaf(Bj[N], tau, A);
     int m0a = floor_split(z0a, &f0a), m0b = floor_split(z0b, &f0b);
@@ -203,21 +203,74 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float
             wa += (m1a > m0a + 1) ? hma : 0.0f;
             wb += (m1b > m0b + 1) ? hmb : 0.0f;
         }
-        acc[j] = fmaf(wa + e1a - e0a, g, acc[j]);
-        acc[N + j] = fmaf(wb + e1b - e0b, g, acc[N + j]);
+        acc2[j].x = fmaf(wa + e1a - e0a, g, acc2[j].x);
+        acc2[j].y = fmaf(wb + e1b - e0b, g, acc2[j].y);
         m0a = m1a; h0a = h1a; e0a = e1a;
         m0b = m1b; h0b = h1b; e0b = e1b;
     }
 }
 
+#ifndef CTGB_FWD_PACKED
+#define CTGB_FWD_PACKED 1
+#endif
+
+// The same sweep with chain a in .x and chain b in .y of float2 pairs, so
+// the boundary positions, fractions, cell values, end terms and row sums
+// of both chains take one packed FMA each; acc2[j] holds rows j and N + j.
+template <int NT, bool MID, int N>
+__device__ __forceinline__ void sweep_rows2_packed(const PatchCells<NT> &H, const float *Bj, float A, float tau,
+                                                   float g, float2 *acc2) {
+    const float2 tau2 = make_float2(tau, tau), A2 = make_float2(A, A), g2 = make_float2(g, g);
+    const float2 neg1 = make_float2(-1.0f, -1.0f), mag = make_float2(-12582912.0f, -12582912.0f);
+    auto o = [&](int t) { return t == 0 ? H.ov0 : (t == 1 ? H.ov1 : (t == 2 ? H.ov2 : H.ov3)); };
+    // h for both chains: NT cells of each chain's row, weighted by the column footprint.
+    auto H2 = [&](int ma, int mb) {
+        const float *pa = H.base + (ma - H.lb) * kPX, *pb = H.base + (mb - H.lb) * kPX;
+        float2 h = __fmul2_rn(make_float2(pa[0], pb[0]), make_float2(o(0), o(0)));
+#pragma unroll
+        for (int t = 1; t < NT; ++t) h = __ffma2_rn(make_float2(pa[t], pb[t]), make_float2(o(t), o(t)), h);
+        return h;
+    };
+    // floor of both boundaries (round-down add of 1.5*2^23) and their fractions.
+    auto split = [&](float2 z, int &ma, int &mb, float2 &fr) {
+        const float ta = __fadd_rd(z.x, 12582912.0f), tb = __fadd_rd(z.y, 12582912.0f);
+        ma = __float_as_int(ta) - 0x4B400000;
+        mb = __float_as_int(tb) - 0x4B400000;
+        const float2 f = __fadd2_rn(make_float2(ta, tb), mag);     // floor as float
+        fr = __ffma2_rn(f, neg1, z);                                // z - floor
+    };
+    float2 z0 = __ffma2_rn(make_float2(Bj[0], Bj[N]), tau2, A2), fr0;
+    int m0a, m0b;
+    split(z0, m0a, m0b, fr0);
+    float2 h0 = H2(m0a, m0b);
+    float2 e0 = __fmul2_rn(h0, fr0);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        const float2 z1 = __ffma2_rn(make_float2(Bj[j + 1], Bj[N + j + 1]), tau2, A2);
+        int m1a, m1b;
+        float2 fr1;
+        split(z1, m1a, m1b, fr1);
+        const float2 h1 = H2(m1a, m1b);
+        const float2 e1 = __fmul2_rn(h1, fr1);
+        float2 w = make_float2((m1a > m0a) ? h0.x : 0.0f, (m1b > m0b) ? h0.y : 0.0f);
+        if (MID) {
+            const float2 hm = H2(m0a + 1, m0b + 1);
+            w = __fadd2_rn(w, make_float2((m1a > m0a + 1) ? hm.x : 0.0f, (m1b > m0b + 1) ? hm.y : 0.0f));
+        }
+        acc2[j] = __ffma2_rn(__fadd2_rn(w, __ffma2_rn(e0, neg1, e1)), g2, acc2[j]);
+        m0a = m1a; m0b = m1b; h0 = h1; e0 = e1;
+    }
+}
+
 template <int NT, bool MID>
 __device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const float *Bj, float A,
-                                           float tau, float g, float *acc) {
+                                           float tau, float g, float2 *acc) {
     PatchCells<NT> H;
     H.base = patch;
     H.lb = lb;
     H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
-    sweep_rows2<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
+    if (CTGB_FWD_PACKED) sweep_rows2_packed<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
+    else sweep_rows2<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
 }
 
 #ifndef CTGB_FWD_MINB
@@ -309,9 +362,9 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     }
     __syncwarp();
 
-    float acc[kTR];
+    float2 acc[kTR / 2];   // rows j (.x) and kTR / 2 + j (.y)
 #pragma unroll
-    for (int j = 0; j < kTR; ++j) acc[j] = 0.0f;
+    for (int j = 0; j < kTR / 2; ++j) acc[j] = make_float2(0.0f, 0.0f);
     uint32_t phase_bits = 0u, pending_bits = 0u;   // bit b: phase parity / TMA outstanding for buffer b
     bool failed = false;
 
@@ -395,7 +448,10 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
                 }
                 __syncwarp();
 #pragma unroll
-                for (int j = 0; j < kTR; ++j) acc[j] = fmaf(spill_rows[j * kTU + lane], g, acc[j]);
+                for (int j = 0; j < kTR / 2; ++j) {
+                    acc[j].x = fmaf(spill_rows[j * kTU + lane], g, acc[j].x);
+                    acc[j].y = fmaf(spill_rows[(kTR / 2 + j) * kTU + lane], g, acc[j].y);
+                }
             }
         }
         __syncwarp();
@@ -421,7 +477,7 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         if (r < nv) {
             const float t2 = (Sz - Pzr[r]) * invD;
             const float K = base * sqrtf(1.0f + t2 * t2) / fabsf(Bj[j + 1] - Bj[j]);
-            proj[((long long)vi * nv + r) * nu + c] = acc[j] * K;
+            proj[((long long)vi * nv + r) * nu + c] = (j < kTR / 2 ? acc[j].x : acc[j - kTR / 2].y) * K;
         }
     }
 }
