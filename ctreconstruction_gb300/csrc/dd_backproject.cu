@@ -292,23 +292,25 @@ __device__ __forceinline__ void integ_voxels(const float2 *__restrict__ IQ, int 
     const float fnv = (float)nv;
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) {
+        // Both ends as one float2: position, floor and fraction in packed
+        // adds (186 ms against 190 ms with scalar ends at 512^3 / 720).
         float vlo, vhi;
+        float2 v2;
         if (LINEAR) {
-            vlo = fmaf((float)j, dlo, lo0);
-            vhi = fmaf((float)j, dhi, hi0);
+            v2 = __ffma2_rn(make_float2((float)j, (float)j), make_float2(dlo, dhi), make_float2(lo0, hi0));
         } else {
             v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &vlo, &vhi);
+            v2 = make_float2(vlo, vhi);
         }
-        const float rw = fast_rcp(vhi - vlo);
-        if (CLAMP) {
-            vlo = fminf(fmaxf(vlo, 0.0f), fnv);
-            vhi = fminf(fmaxf(vhi, 0.0f), fnv);
-        }
-        float flo, fhi;
-        const int mlo = floor_split(vlo, &flo), mhi = floor_split(vhi, &fhi);
+        const float rw = fast_rcp(v2.y - v2.x);
+        if (CLAMP) v2 = make_float2(fminf(fmaxf(v2.x, 0.0f), fnv), fminf(fmaxf(v2.y, 0.0f), fnv));
+        const float2 t2 = __fadd2_rd(v2, make_float2(12582912.0f, 12582912.0f));
+        const int mlo = __float_as_int(t2.x) - 0x4B400000, mhi = __float_as_int(t2.y) - 0x4B400000;
+        const float2 u2 = __ffma2_rn(__fadd2_rn(t2, make_float2(-12582912.0f, -12582912.0f)),
+                                     make_float2(-1.0f, -1.0f), v2);
+        const float ulo = u2.x, uhi = u2.y;
         const float2 *rlo = IQ + mlo * nu + lbase;
         const float2 *rhi = IQ + mhi * nu + lbase;
-        const float ulo = vlo - flo, uhi = vhi - fhi;
         // ov[] carries the view's distance weight; the (C, Q) pairs of each
         // end are summed over the taps with packed FMAs, 2 per tap (190 ms
         // against 196 ms for 4 scalar operations per tap at 512^3 / 720).

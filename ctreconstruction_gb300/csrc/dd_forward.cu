@@ -233,10 +233,10 @@ __device__ __forceinline__ void sweep_rows2_packed(const PatchCells<NT> &H, cons
     };
     // floor of both boundaries (round-down add of 1.5*2^23) and their fractions.
     auto split = [&](float2 z, int &ma, int &mb, float2 &fr) {
-        const float ta = __fadd_rd(z.x, 12582912.0f), tb = __fadd_rd(z.y, 12582912.0f);
-        ma = __float_as_int(ta) - 0x4B400000;
-        mb = __float_as_int(tb) - 0x4B400000;
-        const float2 f = __fadd2_rn(make_float2(ta, tb), mag);     // floor as float
+        const float2 t = __fadd2_rd(z, make_float2(12582912.0f, 12582912.0f));
+        ma = __float_as_int(t.x) - 0x4B400000;
+        mb = __float_as_int(t.y) - 0x4B400000;
+        const float2 f = __fadd2_rn(t, mag);                        // floor as float
         fr = __ffma2_rn(f, neg1, z);                                // z - floor
     };
     float2 z0 = __ffma2_rn(make_float2(Bj[0], Bj[N]), tau2, A2), fr0;
