@@ -261,20 +261,7 @@ __global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__
     const float *__restrict__ q = proj + (long long)v * nu * nv + l;
     float2 *__restrict__ o = out + (long long)v * (nv + 1) * nu + l;
     double c = 0.0;
-    int m = 0;
-    // Eight rows' loads in flight before their sums: one outstanding load
-    // per thread left this pass at a third of the HBM bandwidth.
-    for (; m + 8 <= nv; m += 8) {
-        float x[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) x[k] = __ldg(q + (long long)(m + k) * nu);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            o[(long long)(m + k) * nu] = make_float2((float)c, x[k]);
-            c += x[k];
-        }
-    }
-    for (; m < nv; ++m) {
+    for (int m = 0; m < nv; ++m) {
         const float x = __ldg(q + (long long)m * nu);
         o[(long long)m * nu] = make_float2((float)c, x);
         c += x;
