@@ -201,16 +201,27 @@ class OSSART(_Solver):
 class SolverBatch:
     """Many solvers (scans of uneven sizes) advanced together: one CUDA graph
     holds one iteration of every solver, so a batch iteration is a single
-    graph launch."""
+    graph launch.  Each solver's launches go to a stream of its own, forked
+    from and joined back to the current stream (in the graph: independent
+    branches), so the scans run concurrently — one small scan's launches
+    alone do not fill the GPU."""
 
     def __init__(self, solvers):
         self.solvers = list(solvers)
         self.device = self.solvers[0].device
         self.graph = None
+        self._side = None
 
     def step(self):
-        for s in self.solvers:
-            s.step()
+        main = torch.cuda.current_stream(self.device)
+        if self._side is None:
+            self._side = [torch.cuda.Stream(device=self.device) for _ in self.solvers]
+        for s, st in zip(self.solvers, self._side):
+            st.wait_stream(main)
+            with torch.cuda.stream(st):
+                s.step()
+        for st in self._side:
+            main.wait_stream(st)
 
     def capture(self):
         self.step()
