@@ -276,16 +276,24 @@ __device__ __forceinline__ void sweep_tile(const float *patch, int lb, const flo
 #ifndef CTGB_FWD_MINB
 #define CTGB_FWD_MINB 24
 #endif
+// The views of one launch (relative to view0): every x- (or y-) dominant
+// view of the call goes into one launch, so a scan whose dominant axis
+// alternates every few views still fills the GPU with one grid per axis.
+constexpr int kFwdListViews = 2048;
+struct FwdViewList {
+    int v[kFwdListViews];
+};
+
 template <bool XD, bool TMA>
 __global__ void __launch_bounds__(32, CTGB_FWD_MINB)
 dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
-                      const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0, int vbase,
-                      int ntu, int *status) {
+                      const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0,
+                      const __grid_constant__ FwdViewList views, int ntu, int *status) {
     extern __shared__ __align__(128) unsigned char smraw[];
     FwdTmaSmem &sm = *reinterpret_cast<FwdTmaSmem *>(smraw);
     const TableHeader &h = header(T);
     const int lane = threadIdx.x;
-    const int vi = vbase + blockIdx.x;            // view index relative to view0
+    const int vi = views.v[blockIdx.x];           // view index relative to view0
     const int tu = blockIdx.y % ntu, tv = blockIdx.y / ntu;
     const int c0 = tu * kTU, r0 = tv * kTR;
     const int nu = h.nu, nv = h.nv;
@@ -561,41 +569,53 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
     const float *src_x = d_vol_xzy ? d_vol_xzy : d_vol;
     const long long stk_x = d_vol_xzy ? 1LL : (long long)p->nx;
 
-    // Runs of consecutive views that take the same kernel.
+    // z-dominant views: runs of consecutive views, per-pixel kernel.
     std::vector<int> axes;
     view_axes(p, view0, nviews, axes);
-    int i = 0;
-    while (i < nviews) {
-        const int a = (axes[i] == 2 || !tiles_ok) ? 2 : axes[i];
+    auto axis_of = [&](int i) { return (axes[i] == 2 || !tiles_ok) ? 2 : axes[i]; };
+    for (int i = 0; i < nviews;) {
         int j = i + 1;
-        while (j < nviews && ((axes[j] == 2 || !tiles_ok) ? 2 : axes[j]) == a) ++j;
-        for (int v = i; v < j; v += 65535) {
-            const int n = (j - v) < 65535 ? (j - v) : 65535;
-            if (a == 2) {
+        while (j < nviews && (axis_of(j) == 2) == (axis_of(i) == 2)) ++j;
+        if (axis_of(i) == 2)
+            for (int v = i; v < j; v += 65535) {
+                const int n = (j - v) < 65535 ? (j - v) : 65535;
                 dim3 block(kFwdTileU, kFwdTileV);
                 dim3 grid((p->nu + kFwdTileU - 1) / kFwdTileU, (p->nv + kFwdTileV - 1) / kFwdTileV, n);
                 dd_forward_kernel<<<grid, block, 0, st>>>(T, d_vol, d_vol_xzy, d_proj + (long long)v * view_elems,
                                                           view0 + v);
-            } else {
-                dim3 grid(n, ntu * ntv);
-                if (a == 0) {
-                    if (tma_x)
-                        dd_forward_tma_kernel<true, true><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj,
-                                                                                  view0, v, ntu, status);
-                    else
-                        dd_forward_tma_kernel<true, false><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj,
-                                                                                   view0, v, ntu, status);
-                } else {
-                    if (tma_y)
-                        dd_forward_tma_kernel<false, true><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj,
-                                                                                   view0, v, ntu, status);
-                    else
-                        dd_forward_tma_kernel<false, false><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj,
-                                                                                    view0, v, ntu, status);
-                }
             }
-        }
         i = j;
+    }
+    // x- and y-dominant views: one launch per axis (per kFwdListViews views).
+    for (int a = 0; a < 2; ++a) {
+        FwdViewList list;
+        int n = 0;
+        auto flush = [&]() {
+            if (n == 0) return;
+            dim3 grid(n, ntu * ntv);
+            if (a == 0) {
+                if (tma_x)
+                    dd_forward_tma_kernel<true, true><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj, view0,
+                                                                              list, ntu, status);
+                else
+                    dd_forward_tma_kernel<true, false><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj, view0,
+                                                                               list, ntu, status);
+            } else {
+                if (tma_y)
+                    dd_forward_tma_kernel<false, true><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj, view0,
+                                                                               list, ntu, status);
+                else
+                    dd_forward_tma_kernel<false, false><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj, view0,
+                                                                                list, ntu, status);
+            }
+            n = 0;
+        };
+        for (int i = 0; i < nviews; ++i) {
+            if (axis_of(i) != a) continue;
+            list.v[n++] = i;
+            if (n == kFwdListViews) flush();
+        }
+        flush();
     }
     return check_launch("dd_forward");
 }
@@ -609,14 +629,17 @@ extern "C" int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_
     const bool tiles_ok = (long long)ntu * ntv <= 65535;
     std::vector<int> axes;
     view_axes(p, view0, nviews, axes);
-    int count = 0;
+    auto axis_of = [&](int i) { return (axes[i] == 2 || !tiles_ok) ? 2 : axes[i]; };
+    int count = 0, per_axis[2] = {0, 0};
     for (int i = 0; i < nviews;) {
-        const int a = (axes[i] == 2 || !tiles_ok) ? 2 : axes[i];
         int j = i + 1;
-        while (j < nviews && ((axes[j] == 2 || !tiles_ok) ? 2 : axes[j]) == a) ++j;
-        count += (j - i + 65534) / 65535;
+        while (j < nviews && (axis_of(j) == 2) == (axis_of(i) == 2)) ++j;
+        if (axis_of(i) == 2) count += (j - i + 65534) / 65535;
         i = j;
     }
+    for (int i = 0; i < nviews; ++i)
+        if (axis_of(i) != 2) ++per_axis[axis_of(i)];
+    for (int a = 0; a < 2; ++a) count += (per_axis[a] + kFwdListViews - 1) / kFwdListViews;
     *launches = count;
     return CTGB_OK;
 }

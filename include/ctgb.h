@@ -70,8 +70,9 @@ int ctgb_table_build(const ctgb_params *p, void *host_table, size_t bytes);
  * overwritten.  Stream-ordered; no synchronisation. */
 int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                  float *d_proj, int32_t view0, int32_t nviews, void *stream);
-/* Number of kernel launches ctgb_forward makes for this view range (one per
- * run of consecutive views with the same dominant axis). */
+/* Number of kernel launches ctgb_forward makes for this view range: one for
+ * all x-dominant and one for all y-dominant views (per 2048 views), and one
+ * per run of consecutive z-dominant views. */
 int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_t nviews, int32_t *launches);
 
 /* Same result as ctgb_forward, for callers that cannot allocate device

@@ -133,14 +133,18 @@ def test_product_never_imports_the_oracle():
 
 
 def test_forward_launch_count():
-    """ctgb_forward_launches counts runs of same-axis views: a full circle
-    from theta 0 alternates y, x, y, x, y dominant views (host-only call)."""
+    """ctgb_forward_launches: a full circle from theta 0 alternates y, x, y,
+    x, y dominant views, which take one launch per axis; more than 2048
+    views of one axis take another launch (host-only call)."""
     p = cone_params(n=16, nviews=360, nu=32, nv=24, start=0.0, span=2 * np.pi)
     c = ReconstructionParams.from_dict(p).to_ctgb()
     n = ctypes.c_int32(0)
     _lib.call("ctgb_forward_launches", ctypes.byref(c), 0, 360, ctypes.byref(n))
-    assert n.value == 5
+    assert n.value == 2
     _lib.call("ctgb_forward_launches", ctypes.byref(c), 0, 10, ctypes.byref(n))
     assert n.value == 1
+    c6 = ReconstructionParams.from_dict(cone_params(n=16, nviews=6000, nu=32, nv=24)).to_ctgb()
+    _lib.call("ctgb_forward_launches", ctypes.byref(c6), 0, 6000, ctypes.byref(n))
+    assert n.value == 4     # 3000 views per axis: two launches each
     with pytest.raises(ValueError):
         _lib.call("ctgb_forward_launches", ctypes.byref(c), 350, 20, ctypes.byref(n))
