@@ -699,8 +699,16 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
 // C the running sum of y' = y * K down the column and r_lo, r_hi the voxel's
 // boundaries in row coordinates.  matched_integrate_kernel writes (C, y') as
 // float2; z-dominant views read the raw projections instead.
+// Per view, after the chunk's integrated rows: the forward's boundary slopes
+// Eb[c] = (Sb - Bb[c]) / (Sa - Ba[c]) / db for c = 0 .. nu and the depth
+// factors 1 / (Sa - Pa[c]) for c = 0 .. nu - 1, written once here with the
+// forward's expressions so the backprojector's candidate search reads them
+// instead of dividing per voxel column (the search was most of its time).
+__device__ __forceinline__ int matched_tab_stride(int nu) { return 2 * nu + 2; }
+
 __global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
-                                         float2 *__restrict__ out, int view0, int nviews) {
+                                         float2 *__restrict__ out, float *__restrict__ tabs, int view0,
+                                         int nviews) {
     const TableHeader &h = header(T);
     const int nu = h.nu, nv = h.nv;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -731,6 +739,10 @@ __global__ void matched_integrate_kernel(const float *__restrict__ T, const floa
     const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
     const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
     const float invD = 1.0f / (Sa - Pa[c]);
+    float *__restrict__ tab = tabs + (long long)vi * matched_tab_stride(nu);
+    tab[c] = Eb0;
+    if (c == nu - 1) tab[nu] = Eb1;
+    tab[nu + 1 + c] = invD;
     const float t1 = (Sb - Pb[c]) * invD;
     const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
     float Bprev = (Sz - Bzr[0]) * inv_dz;
@@ -765,8 +777,8 @@ static_assert(kMiTX * kMiTY == 128 && 32 % kMiTX == 0, "bp_matched_integ_kernel:
 
 __global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MI_BLOCKS)
 bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
-                        const float *__restrict__ proj, float *__restrict__ vol, int view0, int nviews, float scale,
-                        int accumulate) {
+                        const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
+                        int view0, int nviews, float scale, int accumulate) {
     const TableHeader &h = header(T);
     const int ix = blockIdx.x * kMiTX + threadIdx.x;
     const int iy = blockIdx.y * kMiTY + threadIdx.y;
@@ -801,9 +813,6 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         const float *__restrict__ pb = T + (xd ? h.off_yplane : h.off_xplane);
         const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
         const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
-        const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
-        const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
-        const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
         const float *__restrict__ Bzr = V + vo.bz;
         const float inv_db = 1.0f / db;
         const float Cb = (Sb - pb[0]) * inv_db;
@@ -828,6 +837,8 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
         const float kf = (float)k;
         // Up to kMC columns with ov_x > 0 (the same x' expressions as the forward).
+        const float *__restrict__ EbT = tabs + (long long)vi * matched_tab_stride(nu);
+        const float *__restrict__ IPT = EbT + nu + 1;
         int ncol = 0;
         int cc[kMC];
         float wcol[kMC], al[kMC], be[kMC];
@@ -835,12 +846,11 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         for (int m = 0; m < kMC; ++m) { cc[m] = 0; wcol[m] = 0.0f; al[m] = 0.0f; be[m] = 0.0f; }
         bool overflow = false;
         for (int c = cA; c <= cB; ++c) {
-            const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
-            const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
+            const float Eb0 = __ldg(EbT + c), Eb1 = __ldg(EbT + c + 1);
             const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
             const float ovx = fminf(kf + 1.0f, fmaxf(xa, xb)) - fmaxf(kf, fminf(xa, xb));
             if (!(ovx > 0.0f)) continue;
-            const float tau = q * (1.0f / (Sa - Pa[c]));
+            const float tau = q * __ldg(IPT + c);
             // voxel boundary z' -> row coordinate: r = ((z' - A) / tau - B0) / dB
             const float inv = 1.0f / (tau * dB);
             const float wz = fabsf(dB * tau);
@@ -992,7 +1002,9 @@ extern "C" int ctgb_backproject_fdk_workspace_bytes(const ctgb_params *p, int32_
     clear_error();
     if (!p || !bytes || nviews < 0 || p->nu < 1 || p->nv < 1)
         return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_workspace_bytes: bad arguments");
-    *bytes = (size_t)nviews * (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    // integrated rows, plus the matched backprojector's per-view column tables
+    *bytes = (size_t)nviews * ((size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2) +
+                               (size_t)(2 * p->nu + 2) * sizeof(float));
     return CTGB_OK;
 }
 
@@ -1086,7 +1098,8 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
         }
         return CTGB_OK;
     }
-    const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    const size_t rows_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
+    const size_t per_view = rows_view + (size_t)(2 * p->nu + 2) * sizeof(float);
     const int chunk = (int)(workspace_bytes / per_view);
     if (chunk < 1) return set_error(CTGB_ERR_SIZE, "ctgb_backproject_matched_ws: workspace below one view");
     const float *T = static_cast<const float *>(d_table);
@@ -1097,9 +1110,11 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
         const int n = nviews - v < chunk ? nviews - v : chunk;
         const long long threads = (long long)p->nu * n;
         const float *pv = d_proj + (long long)v * p->nu * p->nv;
-        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, pv, ws, view0 + v, n);
+        // the chunk's n views of integrated rows, then their column tables
+        float *tabs = reinterpret_cast<float *>(ws + (size_t)n * (p->nv + 1) * p->nu);
+        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, pv, ws, tabs, view0 + v, n);
         const int acc = (v > 0) ? 1 : accumulate;
-        bp_matched_integ_kernel<<<grid, block, 0, s>>>(T, ws, pv, d_vol, view0 + v, n, scale, acc);
+        bp_matched_integ_kernel<<<grid, block, 0, s>>>(T, ws, tabs, pv, d_vol, view0 + v, n, scale, acc);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_integ_kernel: %s", cudaGetErrorString(e));
