@@ -107,6 +107,8 @@ int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, const float 
  * lookups per detector column.  Views are processed in chunks that fit the
  * workspace (at least one view: ctgb_backproject_fdk_workspace_bytes(p, 1, ..)).
  * Replaces the same reference code as ctgb_backproject_fdk. */
+/* Workspace bytes for nviews views of ctgb_backproject_fdk_ws and of
+ * ctgb_backproject_matched_ws (the latter's per-view tables included). */
 int ctgb_backproject_fdk_workspace_bytes(const ctgb_params *p, int32_t nviews, size_t *bytes);
 int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                             int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
@@ -130,8 +132,10 @@ int ctgb_backproject_fdk_integrated(const ctgb_params *p, const void *d_table, c
 int ctgb_backproject_matched(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                              int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
 /* Same result, faster: projections prescaled by the forward's per-pixel
- * factor and integrated along v into a caller-supplied workspace (size as for
- * ctgb_backproject_fdk_workspace_bytes), processed in view chunks that fit. */
+ * factor and integrated along v into a caller-supplied workspace, with a
+ * per-view table of the forward's detector-column slopes and depth factors
+ * after them (size per view from ctgb_backproject_fdk_workspace_bytes, which
+ * counts both), processed in view chunks that fit. */
 int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                                 int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
                                 size_t workspace_bytes, void *stream);
