@@ -211,6 +211,20 @@ struct FanBatchHeader {
     int64_t off_slices, off_items;     // in 4-byte words from the base
 };
 
+// Linear interpolation of one sinogram row at channel position f
+// (interp1d(kind='linear', bounds_error=False, fill_value=0)).
+__device__ __forceinline__ float fan_sample(const float *__restrict__ row, float f, float last, int nch) {
+    if (!(f >= 0.0f && f <= last)) return 0.0f;
+    const int k = min((int)f, nch - 2);
+    const float fr = f - (float)k;
+    const float a = __ldg(row + k), b = __ldg(row + k + 1);
+    return fmaf(fr, b - a, a);
+}
+
+// Each thread owns two pixels of an item's tile, rows j and j + blockDim.y
+// of the same column, so the per-view geometry of both (t, s, the
+// interpolation position and the distance weight) runs on packed f32x2
+// operations; the launch uses tile_y / 2 thread rows for a tile_y-row tile.
 __global__ void fan_bp_kernel(const int *__restrict__ B, const float *__restrict__ sino, float *__restrict__ images,
                               int accumulate) {
     extern __shared__ float2 cs[];     // (cos, sin) per view of the current item's slice
@@ -228,44 +242,53 @@ __global__ void fan_bp_kernel(const int *__restrict__ B, const float *__restrict
             cs[v] = make_float2(cv, sv);
         }
         __syncthreads();
-        const int i = w.y + threadIdx.x, j = w.z + threadIdx.y;
-        if (i >= sl.nx || j >= sl.ny) continue;
-        const float x = sl.x0 + i * sl.dx, y = sl.y0 + j * sl.dy;
+        const int i = w.y + threadIdx.x, j0 = w.z + threadIdx.y, j1 = j0 + blockDim.y;
+        // the second row only inside this item's tile (odd tile heights)
+        const bool in0 = i < sl.nx && j0 < sl.ny;
+        const bool in1 = i < sl.nx && j1 < sl.ny && (int)(threadIdx.y + blockDim.y) < h.tile_y;
+        if (!in0) continue;             // row j1 > j0: nothing in this thread's column either
+        const float x = sl.x0 + i * sl.dx;
+        const float2 y2 = make_float2(sl.y0 + j0 * sl.dy, sl.y0 + j1 * sl.dy);
         const float *__restrict__ q = sino + sl.sino_offset;
         const float inv_dg = 1.0f / sl.dg, inv_D = 1.0f / sl.D;
         const float last = (float)(sl.nch - 1);
-        float acc = 0.0f;
+        const float2 R2 = make_float2(sl.R, sl.R), m1 = make_float2(-1.0f, -1.0f);
+        float acc0 = 0.0f, acc1 = 0.0f;
         // Fast reciprocals (a few ulp) instead of IEEE divides: well inside
         // the 1e-4 agreement with the FP64 restatement.
         for (int v = 0; v < sl.nviews; ++v) {
             const float2 c = cs[v];
-            const float t = x * c.x + y * c.y;
-            const float s = -x * c.y + y * c.x;
-            float f, wgt;
+            // t = x cos + y sin, s = -x sin + y cos for both pixels
+            const float2 t2 = __ffma2_rn(y2, make_float2(c.y, c.y), make_float2(x * c.x, x * c.x));
+            const float2 s2 = __ffma2_rn(y2, make_float2(c.x, c.x), make_float2(-x * c.y, -x * c.y));
+            const float2 den = __ffma2_rn(s2, m1, R2);
+            float2 f, wgt;
             if (sl.arc) {
                 // matlab/FanBeamReconArc.m:37-44: gamma' = atan(t / (R - s)), 1 / L^2.
-                const float den = sl.R - s;
-                f = (atan2f(t, den) - sl.g0) * inv_dg;
-                wgt = __fdividef(1.0f, fmaf(den, den, t * t));
+                f = make_float2((atan2f(t2.x, den.x) - sl.g0) * inv_dg, (atan2f(t2.y, den.y) - sl.g0) * inv_dg);
+                const float2 L2 = __ffma2_rn(den, den, __fmul2_rn(t2, t2));
+                wgt = make_float2(__fdividef(1.0f, L2.x), __fdividef(1.0f, L2.y));
             } else {
                 // FanBeam.py:123-129: InterpX = R t / (R - s); U = (D - s) / D.
-                const float den = sl.R - s;
-                f = fmaf(sl.R * t, __fdividef(1.0f, den), -sl.g0) * inv_dg;
-                const float U = (sl.D - s) * inv_D;
-                wgt = __fdividef(1.0f, U * U);
+                const float2 rden = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+                f = __fmul2_rn(__ffma2_rn(__fmul2_rn(R2, t2), rden, make_float2(-sl.g0, -sl.g0)),
+                               make_float2(inv_dg, inv_dg));
+                const float2 U = __fmul2_rn(__ffma2_rn(s2, m1, make_float2(sl.D, sl.D)), make_float2(inv_D, inv_D));
+                const float2 UU = __fmul2_rn(U, U);
+                wgt = make_float2(__fdividef(1.0f, UU.x), __fdividef(1.0f, UU.y));
             }
-            // interp1d(kind='linear', bounds_error=False, fill_value=0)
-            if (f >= 0.0f && f <= last) {
-                const int k = min((int)f, sl.nch - 2);
-                const float fr = f - (float)k;
-                const float* row = q + (long long)v * sl.nch;
-                const float a = __ldg(row + k), b = __ldg(row + k + 1);
-                acc = fmaf(fmaf(fr, b - a, a), wgt, acc);
-            }
+            const float *__restrict__ row = q + (long long)v * sl.nch;
+            acc0 = fmaf(fan_sample(row, f.x, last, sl.nch), wgt.x, acc0);
+            if (in1) acc1 = fmaf(fan_sample(row, f.y, last, sl.nch), wgt.y, acc1);
         }
-        float *dst = images + sl.image_offset + (long long)j * sl.nx + i;
-        const float val = acc * sl.dtheta;
-        *dst = accumulate ? *dst + val : val;
+        float *dst = images + sl.image_offset + (long long)j0 * sl.nx + i;
+        const float val0 = acc0 * sl.dtheta;
+        *dst = accumulate ? *dst + val0 : val0;
+        if (in1) {
+            float *dst1 = images + sl.image_offset + (long long)j1 * sl.nx + i;
+            const float val1 = acc1 * sl.dtheta;
+            *dst1 = accumulate ? *dst1 + val1 : val1;
+        }
     }
 }
 
@@ -345,7 +368,10 @@ extern "C" int ctgb_fan_backproject(const void *d_batch, int32_t max_views, cons
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fan_bp smem: %s", cudaGetErrorString(e));
         attr = true;
     }
-    fan_bp_kernel<<<grid_blocks, dim3(tile_x, tile_y), smem, static_cast<cudaStream_t>(stream)>>>(
+    // two pixel rows per thread: tile_y / 2 thread rows (a tile of one row
+    // keeps one thread row and its second pixel falls outside the tile)
+    const int rows = tile_y > 1 ? (tile_y + 1) / 2 : 1;
+    fan_bp_kernel<<<grid_blocks, dim3(tile_x, rows), smem, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const int *>(d_batch), d_sino, d_images, accumulate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fan_bp_kernel: %s", cudaGetErrorString(e));
