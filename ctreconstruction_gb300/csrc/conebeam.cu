@@ -45,7 +45,8 @@ __device__ __forceinline__ void lin_weights(float xq, float x0, float inv_dx, co
     const int lc = min(max(l, 0), n - 1), hc = min(max(h, 0), n - 1);
     float w1 = xq - grid[lc], w2 = grid[hc] - xq;
     if (fabsf(w1) < 1e-4f && fabsf(w2) < 1e-4f) w1 = 1.0f;
-    const float inv = 1.0f / (w1 + w2);
+    // fast reciprocal (a few ulp; w1 + w2 is the grid pitch or 1 + w2)
+    const float inv = __fdividef(1.0f, w1 + w2);
     *lo = lc; *hi = hc;
     *a = w2 * inv; *b = w1 * inv;
 }
