@@ -753,65 +753,101 @@ __global__ void head_grad_kernel(const float *__restrict__ gy, const __nv_bfloat
 
 // Weight gradient of a 3x3x3 convolution (zero padding):
 //   dW[tap][co][ci] = sum_v g[v][co] * x[v + offset(tap)][ci]
-// Block (chunk, tap): voxels [chunk * kWgChunk, ...) staged 32 at a time in
-// shared memory as fp32; each thread owns (co, ci) pairs tid, tid + 256, ...
-// (at most kWgPairs).  Per-block partials -> partials[chunk][tap][co][ci].
-constexpr int kWgChunk = 8192, kWgVox = 32, kWgPairs = 24;
+// The voxels are cut into x-row segments of at most kWgSeg voxels; a chunk
+// is kWgSegs consecutive segments.  Block (chunk, dz, pair group): per
+// segment, the output gradient g of the segment and the three input rows at
+// (z + dz, y - 1 .. y + 1) over the segment plus one voxel each side are
+// staged in shared memory as fp32; each thread owns at most kWgPairs
+// (co, ci) pairs of the group and, for the 9 (dy, dx) taps of its dz,
+// slides a three-voxel window along x, so each voxel costs it one g read and
+// three x reads for nine FMAs per pair.  Per-block partials ->
+// partials[chunk][tap][co][ci] (every block writes its 9 taps).
+constexpr int kWgSeg = 64, kWgSegs = 64, kWgThreads = 256, kWgPairs = 2;
 
-__global__ void __launch_bounds__(256) wgrad_kernel(const __nv_bfloat16 *__restrict__ x, int cin,
-                                                    const __nv_bfloat16 *__restrict__ g, int cout,
-                                                    float *__restrict__ partials, int N, int D, int H, int W) {
+__device__ __forceinline__ void wgrad_segments(long long nseg, int segs_per_row, int W, int *sx0, int *slen,
+                                               long long seg, long long *row) {
+    *row = seg / segs_per_row;
+    *sx0 = (int)(seg - *row * segs_per_row) * kWgSeg;
+    *slen = min(kWgSeg, W - *sx0);
+}
+
+__global__ void __launch_bounds__(kWgThreads) wgrad_kernel(const __nv_bfloat16 *__restrict__ x, int cin,
+                                                           const __nv_bfloat16 *__restrict__ g, int cout,
+                                                           float *__restrict__ partials, int N, int D, int H,
+                                                           int W) {
     extern __shared__ float wsm[];
-    float *gs = wsm;                     // [kWgVox][cout]
-    float *xs = wsm + kWgVox * cout;     // [kWgVox][cin]
-    const int chunk = blockIdx.x, tap = blockIdx.y;
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    const long long V = (long long)N * D * H * W;
-    const long long v0 = (long long)chunk * kWgChunk;
-    const long long v1 = min(V, v0 + kWgChunk);
+    float *gs = wsm;                               // [kWgSeg][cout]
+    float *xs = wsm + kWgSeg * cout;               // [3][kWgSeg + 2][cin]
+    const int chunk = blockIdx.x, dzi = blockIdx.y, pgroup = blockIdx.z;
+    const int dz = dzi - 1;
+    const int segs_per_row = (W + kWgSeg - 1) / kWgSeg;
+    const long long nseg = (long long)N * D * H * segs_per_row;
+    const long long s0 = (long long)chunk * kWgSegs, s1 = min(nseg, s0 + kWgSegs);
     const int npairs = cout * cin;
-    float acc[kWgPairs];
+    int co[kWgPairs], ci[kWgPairs];
+    bool has[kWgPairs];
 #pragma unroll
-    for (int k = 0; k < kWgPairs; ++k) acc[k] = 0.0f;
-    for (long long vb = v0; vb < v1; vb += kWgVox) {
-        __syncthreads();
-        for (int e = threadIdx.x; e < kWgVox * cout; e += blockDim.x) {
-            const long long v = vb + e / cout;
-            gs[e] = v < v1 ? __bfloat162float(g[v * cout + e % cout]) : 0.0f;
-        }
-        for (int e = threadIdx.x; e < kWgVox * cin; e += blockDim.x) {
-            const long long v = vb + e / cin;
+    for (int k = 0; k < kWgPairs; ++k) {
+        const int p = (pgroup * kWgPairs + k) * kWgThreads + threadIdx.x;
+        has[k] = p < npairs;
+        co[k] = has[k] ? p / cin : 0;
+        ci[k] = has[k] ? p % cin : 0;
+    }
+    float acc[kWgPairs][9];
+#pragma unroll
+    for (int k = 0; k < kWgPairs; ++k)
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[k][t] = 0.0f;
+    const int SX = kWgSeg + 2;
+    for (long long sg = s0; sg < s1; ++sg) {
+        long long row;
+        int sx0, slen;
+        wgrad_segments(nseg, segs_per_row, W, &sx0, &slen, sg, &row);
+        const int yy = (int)(row % H), zz = (int)((row / H) % D), nn = (int)(row / ((long long)H * D));
+        __syncthreads();                           // the previous segment's reads are done
+        const __nv_bfloat16 *grow = g + ((((long long)nn * D + zz) * H + yy) * W + sx0) * cout;
+        for (int e = threadIdx.x; e < kWgSeg * cout; e += kWgThreads)
+            gs[e] = e < slen * cout ? __bfloat162float(grow[e]) : 0.0f;
+        const int z2 = zz + dz;
+        for (int e = threadIdx.x; e < 3 * SX * cin; e += kWgThreads) {
+            const int c = e % cin, xi = (e / cin) % SX, dyi = e / (cin * SX);
+            const int y2 = yy + dyi - 1, x2 = sx0 + xi - 1;
             float val = 0.0f;
-            if (v < v1) {
-                long long r = v;
-                const int xx = (int)(r % W) + dx;
-                r /= W;
-                const int yy = (int)(r % H) + dy;
-                r /= H;
-                const int zz = (int)(r % D) + dz;
-                const int n = (int)(r / D);
-                if (xx >= 0 && xx < W && yy >= 0 && yy < H && zz >= 0 && zz < D)
-                    val = __bfloat162float(x[((((long long)n * D + zz) * H + yy) * W + xx) * cin + e % cin]);
-            }
+            if (z2 >= 0 && z2 < D && y2 >= 0 && y2 < H && x2 >= 0 && x2 < W && xi <= slen + 1)
+                val = __bfloat162float(x[((((long long)nn * D + z2) * H + y2) * W + x2) * cin + c]);
             xs[e] = val;
         }
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kWgPairs; ++k) {
-            const int p = threadIdx.x + k * 256;
-            if (p < npairs) {
-                const int co = p / cin, ci = p % cin;
-                float s = acc[k];
-                for (int j = 0; j < kWgVox; ++j) s = fmaf(gs[j * cout + co], xs[j * cin + ci], s);
-                acc[k] = s;
+            if (!has[k]) continue;
+            float w0[3], w1[3];                    // x[v - 1], x[v] per dy row
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy) {
+                w0[dy] = xs[(dy * SX + 0) * cin + ci[k]];
+                w1[dy] = xs[(dy * SX + 1) * cin + ci[k]];
+            }
+            for (int v = 0; v < slen; ++v) {
+                const float gv = gs[v * cout + co[k]];
+#pragma unroll
+                for (int dy = 0; dy < 3; ++dy) {
+                    const float w2 = xs[(dy * SX + v + 2) * cin + ci[k]];
+                    acc[k][dy * 3 + 0] = fmaf(gv, w0[dy], acc[k][dy * 3 + 0]);
+                    acc[k][dy * 3 + 1] = fmaf(gv, w1[dy], acc[k][dy * 3 + 1]);
+                    acc[k][dy * 3 + 2] = fmaf(gv, w2, acc[k][dy * 3 + 2]);
+                    w0[dy] = w1[dy];
+                    w1[dy] = w2;
+                }
             }
         }
     }
-    float *dst = partials + ((long long)chunk * 27 + tap) * npairs;
 #pragma unroll
     for (int k = 0; k < kWgPairs; ++k) {
-        const int p = threadIdx.x + k * 256;
-        if (p < npairs) dst[p] = acc[k];
+        if (!has[k]) continue;
+        const int p = co[k] * cin + ci[k];
+#pragma unroll
+        for (int t = 0; t < 9; ++t)
+            partials[((long long)chunk * 27 + dzi * 9 + t) * npairs + p] = acc[k][t];
     }
 }
 
@@ -1110,21 +1146,32 @@ extern "C" int ctgb_unet_head_grad(const float *gy, const void *a, const float *
 extern "C" int ctgb_unet_wgrad_chunks(int32_t n, int32_t d, int32_t h, int32_t w, int32_t *chunks) {
     clear_error();
     if (!chunks || n < 1 || d < 1 || h < 1 || w < 1) return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad_chunks: bad arguments");
-    const long long V = (long long)n * d * h * w;
-    *chunks = (int)((V + kWgChunk - 1) / kWgChunk);
+    const long long nseg = (long long)n * d * h * ((w + kWgSeg - 1) / kWgSeg);
+    const long long c = (nseg + kWgSegs - 1) / kWgSegs;
+    if (c > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "ctgb_unet_wgrad_chunks: volume too large");
+    *chunks = (int)c;
     return CTGB_OK;
 }
 
 extern "C" int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, float *partials, int32_t n,
                                int32_t d, int32_t h, int32_t w, void *stream) {
     clear_error();
-    if (!x || !g || !partials || cin < 1 || cout < 1 || cin * cout > 256 * kWgPairs || n < 1)
+    if (!x || !g || !partials || cin < 1 || cout < 1 || cin * cout > 6144 || n < 1 || d < 1 || h < 1 || w < 1)
         return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: bad arguments");
-    const long long V = (long long)n * d * h * w;
-    const int chunks = (int)((V + kWgChunk - 1) / kWgChunk);
-    const size_t smem = sizeof(float) * kWgVox * (size_t)(cin + cout);
-    dim3 grid(chunks, 27);
-    wgrad_kernel<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(
+    int chunks = 0;
+    if (int st = ctgb_unet_wgrad_chunks(n, d, h, w, &chunks)) return st;
+    const int pgroups = (cin * cout + kWgThreads * kWgPairs - 1) / (kWgThreads * kWgPairs);
+    const size_t smem = sizeof(float) * ((size_t)kWgSeg * cout + 3 * (size_t)(kWgSeg + 2) * cin);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(sizeof(float) * (kWgSeg * 96 + 3 * (kWgSeg + 2) * 96)));
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "wgrad smem attribute: %s", cudaGetErrorString(e));
+        attr = true;
+    }
+    if (cin > 96 || cout > 96) return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: at most 96 channels");
+    dim3 grid(chunks, 3, pgroups);
+    wgrad_kernel<<<grid, kWgThreads, smem, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const __nv_bfloat16 *>(x), cin, static_cast<const __nv_bfloat16 *>(g), cout, partials, n, d, h,
         w);
     return ew_done("wgrad_kernel");

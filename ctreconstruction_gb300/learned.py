@@ -306,31 +306,61 @@ def random_patches(pairs, size, count, generator):
     return torch.stack(pre).contiguous(), torch.stack(post).contiguous()
 
 
-def train(net, pairs, steps=200, batch=4, size=(32, 32, 64), lr=1e-3, seed=0, scale=None, log_every=0):
+def train(net, pairs, steps=200, batch=4, size=(32, 32, 64), lr=1e-3, seed=0, scale=None, log_every=0,
+          graph=True):
     """Fit net(pre) ~ post by MSE with Adam (fp32 master weights).  scale:
     the per-sample input scale (default: the pairs' mean absolute pre value).
-    Returns the loss history."""
+    Returns the loss history.
+
+    graph: after one eager step, the whole step — the bf16 weight blocks,
+    forward, loss, backward and the Adam update — is captured in a CUDA graph
+    and replayed, the batch being copied into the graph's static input
+    buffers; the results are the eager steps' bit for bit (the same kernels
+    in the same order), without the host launching some 200 small kernels
+    and torch ops per step.  Losses stay on the device until the end."""
     gen = torch.Generator().manual_seed(seed)
     params = list(net.params.values())
-    opt = torch.optim.Adam(params, lr=lr)
+    dev = net.device
+    # the device-side (capturable) Adam in both modes, so eager and graph
+    # steps do the same arithmetic
+    opt = torch.optim.Adam(params, lr=lr, capturable=True)
     if scale is None:
         scale = float(torch.stack([p[0].abs().mean() for p in pairs]).mean().clamp(min=1e-12))
-    losses = []
-    for it in range(steps):
-        pre, post = random_patches(pairs, size, batch, gen)
-        pre, post = pre.to(net.device), post.to(net.device)
-        y = net.forward(pre, torch.full((batch,), scale, device=net.device), keep=True)
-        diff = y - post
-        loss = float((diff * diff).mean()) / scale ** 2
-        gy = 2.0 * diff / diff.numel() / scale ** 2
+    pre_s = torch.empty((batch,) + tuple(size), dtype=torch.float32, device=dev)
+    post_s = torch.empty_like(pre_s)
+    scale_t = torch.full((batch,), scale, dtype=torch.float32, device=dev)
+    loss_s = torch.zeros((), dtype=torch.float32, device=dev)
+    inv_s2 = 1.0 / scale ** 2
+
+    def step():
+        y = net.forward(pre_s, scale_t, keep=True)
+        diff = y - post_s
+        loss_s.copy_((diff * diff).mean() * inv_s2)
+        gy = diff * (2.0 * inv_s2 / diff.numel())
         grads = net.backward(gy)
         for k, p in net.params.items():
             p.grad = grads[k]
         opt.step()
-        opt.zero_grad(set_to_none=True)
-        losses.append(loss)
+
+    g = None
+    losses = []
+    for it in range(steps):
+        pre, post = random_patches(pairs, size, batch, gen)
+        pre_s.copy_(pre)
+        post_s.copy_(post)
+        if graph and it > 0:
+            if g is None:
+                torch.cuda.synchronize(dev)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    step()
+            g.replay()
+        else:
+            step()
+        losses.append(loss_s.clone())
         if log_every and it % log_every == 0:
-            print("step %d loss %.4e" % (it, loss))
+            print("step %d loss %.4e" % (it, float(losses[-1])))
+    losses = [float(v) for v in torch.stack(losses).cpu()] if losses else []
     net.scale = scale
     return losses
 

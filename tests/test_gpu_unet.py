@@ -187,6 +187,24 @@ def test_training_reduces_loss(cuda):
     assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:3])
 
 
+def test_graph_training_matches_eager(cuda):
+    """The graph-replayed training step gives the eager steps' losses and
+    parameters bit for bit."""
+    gen = torch.Generator(device=cuda).manual_seed(2)
+    pairs = []
+    for _ in range(3):
+        v = torch.rand((16, 32, 64), device=cuda, generator=gen) * 0.02
+        pairs.append((v, F.avg_pool3d(v[None, None], 3, stride=1, padding=1, count_include_pad=False)[0, 0]))
+    runs = []
+    for graph in (False, True):
+        net = UNet3D(device=cuda, seed=4)
+        losses = train(net, pairs, steps=6, batch=2, size=(8, 32, 64), lr=2e-3, seed=1, graph=graph)
+        runs.append((losses, {k: v.detach().clone() for k, v in net.params.items()}))
+    assert runs[0][0] == runs[1][0]
+    for k in runs[0][1]:
+        assert torch.equal(runs[0][1][k], runs[1][1][k]), k
+
+
 def test_learned_asd_pocs_small(cuda):
     """The whole learned path at 64^3 / 30 views: pairs from ASD-POCS itself,
     a short training run, then ASD-POCS with the learned step (judged by the
