@@ -805,17 +805,28 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_kernel(const __nv_bfloat16 *
         wgrad_segments(nseg, segs_per_row, W, &sx0, &slen, sg, &row);
         const int yy = (int)(row % H), zz = (int)((row / H) % D), nn = (int)(row / ((long long)H * D));
         __syncthreads();                           // the previous segment's reads are done
+        // 8 channels (16 bytes) per staged item; channel counts are multiples of 8
         const __nv_bfloat16 *grow = g + ((((long long)nn * D + zz) * H + yy) * W + sx0) * cout;
-        for (int e = threadIdx.x; e < kWgSeg * cout; e += kWgThreads)
-            gs[e] = e < slen * cout ? __bfloat162float(grow[e]) : 0.0f;
-        const int z2 = zz + dz;
-        for (int e = threadIdx.x; e < 3 * SX * cin; e += kWgThreads) {
-            const int c = e % cin, xi = (e / cin) % SX, dyi = e / (cin * SX);
+        const int gv8 = cout / 8;
+        for (int e = threadIdx.x; e < kWgSeg * gv8; e += kWgThreads) {
+            float f[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            if (e < slen * gv8) unpack8(__ldg(reinterpret_cast<const uint4 *>(grow) + e), f);
+            float4 *dstg = reinterpret_cast<float4 *>(gs + e * 8);
+            dstg[0] = make_float4(f[0], f[1], f[2], f[3]);
+            dstg[1] = make_float4(f[4], f[5], f[6], f[7]);
+        }
+        const int z2 = zz + dz, xv8 = cin / 8;
+        for (int e = threadIdx.x; e < 3 * SX * xv8; e += kWgThreads) {
+            const int c8 = e % xv8, r = e / xv8, xi = r % SX, dyi = r / SX;
             const int y2 = yy + dyi - 1, x2 = sx0 + xi - 1;
-            float val = 0.0f;
+            float f[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             if (z2 >= 0 && z2 < D && y2 >= 0 && y2 < H && x2 >= 0 && x2 < W && xi <= slen + 1)
-                val = __bfloat162float(x[((((long long)nn * D + z2) * H + y2) * W + x2) * cin + c]);
-            xs[e] = val;
+                unpack8(__ldg(reinterpret_cast<const uint4 *>(x + ((((long long)nn * D + z2) * H + y2) * W + x2) * cin) +
+                              c8),
+                        f);
+            float4 *dstx = reinterpret_cast<float4 *>(xs + (size_t)r * cin + c8 * 8);
+            dstx[0] = make_float4(f[0], f[1], f[2], f[3]);
+            dstx[1] = make_float4(f[4], f[5], f[6], f[7]);
         }
         __syncthreads();
 #pragma unroll
@@ -1156,8 +1167,9 @@ extern "C" int ctgb_unet_wgrad_chunks(int32_t n, int32_t d, int32_t h, int32_t w
 extern "C" int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, float *partials, int32_t n,
                                int32_t d, int32_t h, int32_t w, void *stream) {
     clear_error();
-    if (!x || !g || !partials || cin < 1 || cout < 1 || cin * cout > 6144 || n < 1 || d < 1 || h < 1 || w < 1)
-        return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: bad arguments");
+    if (!x || !g || !partials || cin < 8 || cout < 8 || cin % 8 || cout % 8 || cin * cout > 6144 || n < 1 || d < 1 ||
+        h < 1 || w < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: bad arguments (channels: multiples of 8)");
     int chunks = 0;
     if (int st = ctgb_unet_wgrad_chunks(n, d, h, w, &chunks)) return st;
     const int pgroups = (cin * cout + kWgThreads * kWgPairs - 1) / (kWgThreads * kWgPairs);

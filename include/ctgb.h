@@ -319,7 +319,8 @@ int ctgb_unet_head_grad(const float *gy, const void *a, const float *wb, const f
                         float *partials, int32_t n, int64_t vps, void *stream);
 /* Weight gradient of one input segment: partials[chunk][27][cout][cin] of
  * sum_v g[v][co] x[v + tap][ci] (chunks from ctgb_unet_wgrad_chunks; the
- * caller sums over chunks).  cin, cout <= 96 and cin * cout <= 6144. */
+ * caller sums over chunks).  cin, cout multiples of 8, at most 96, and
+ * cin * cout <= 6144. */
 int ctgb_unet_wgrad_chunks(int32_t n, int32_t d, int32_t h, int32_t w, int32_t *chunks);
 int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, float *partials, int32_t n, int32_t d,
                     int32_t h, int32_t w, void *stream);
