@@ -838,6 +838,7 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_kernel(const __nv_bfloat16 *
                 w0[dy] = xs[(dy * SX + 0) * cin + ci[k]];
                 w1[dy] = xs[(dy * SX + 1) * cin + ci[k]];
             }
+#pragma unroll 4
             for (int v = 0; v < slen; ++v) {
                 const float gv = gs[v * cout + co[k]];
 #pragma unroll
