@@ -369,13 +369,9 @@ extern "C" int ctgb_fan_backproject(const void *d_batch, int32_t max_views, cons
         max_views < 1 || max_views > 8192)
         return set_error(CTGB_ERR_ARG, "ctgb_fan_backproject: bad arguments");
     const size_t smem = (size_t)max_views * sizeof(float2);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(fan_bp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(8192 * sizeof(float2)));
-        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fan_bp smem: %s", cudaGetErrorString(e));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t ea = smem_limit_once((const void *)fan_bp_kernel, (int)(8192 * sizeof(float2)), attr);
+    if (ea != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fan_bp smem: %s", cudaGetErrorString(ea));
     // two pixel rows per thread: tile_y / 2 thread rows (a tile of one row
     // keeps one thread row and its second pixel falls outside the tile)
     const int rows = tile_y > 1 ? (tile_y + 1) / 2 : 1;

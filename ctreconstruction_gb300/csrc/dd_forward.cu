@@ -518,19 +518,14 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
     int *status = ctgb_status_ptr();
     if (!status) return set_error(CTGB_ERR_CUDA, "ctgb_forward: device status word unavailable");
     const int smem = (int)sizeof(FwdTmaSmem);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaSuccess;
-        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<true, true>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
-        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<false, true>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
-        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<true, false>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
-        e = (e == cudaSuccess) ? cudaFuncSetAttribute(dd_forward_tma_kernel<false, false>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem) : e;
+    static std::atomic<unsigned long long> attr[4];
+    const void *kernels[4] = {(const void *)dd_forward_tma_kernel<true, true>,
+                              (const void *)dd_forward_tma_kernel<false, true>,
+                              (const void *)dd_forward_tma_kernel<true, false>,
+                              (const void *)dd_forward_tma_kernel<false, false>};
+    for (int k = 0; k < 4; ++k) {
+        cudaError_t e = smem_limit_once(kernels[k], smem, attr[k]);
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "dd_forward smem attribute: %s", cudaGetErrorString(e));
-        attr_set = true;
     }
     const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + kTR - 1) / kTR;
     const bool tiles_ok = (long long)ntu * ntv <= 65535;

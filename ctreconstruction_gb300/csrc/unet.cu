@@ -893,13 +893,9 @@ template <int COUT, int CMAX, int EPI>
 static int launch_conv(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &b0, const CUtensorMap &b1,
                        const ConvGeom &g, const float *bias, void *out, cudaStream_t st) {
     using Cfg = ConvCfg<COUT, CMAX>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_kernel<COUT, CMAX, EPI>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
-        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t ea = smem_limit_once((const void *)conv3d_tc_kernel<COUT, CMAX, EPI>, Cfg::kSmem, attr);
+    if (ea != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(ea));
     int *status = ctgb_status_ptr();
     if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
     const long long tiles = (long long)g.N * g.D * (g.H / g.R) * (g.W / g.Wb);
@@ -926,13 +922,9 @@ static int launch_conv_dx_res(const CUtensorMap &a0, const CUtensorMap &a1, cons
     if constexpr (kSmemMax > kDxSmemLimit) {
         return set_error(CTGB_ERR_ARG, "conv3d: tap-reuse shape above the shared-memory limit");
     } else {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(conv3d_tc_dx_kernel<COUT, CMAX, EPI, RES>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax);
-        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(e));
-        attr = true;
-    }
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t ea = smem_limit_once((const void *)conv3d_tc_dx_kernel<COUT, CMAX, EPI, RES>, kSmemMax, attr);
+    if (ea != cudaSuccess) return set_error(CTGB_ERR_CUDA, "conv3d smem attribute: %s", cudaGetErrorString(ea));
     int *status = ctgb_status_ptr();
     if (!status) return set_error(CTGB_ERR_CUDA, "device status word unavailable");
     const long long tiles = (long long)g.N * g.D * ((g.H + Cfg::kR - 1) / Cfg::kR) * (g.W / kCvM);
@@ -1175,14 +1167,11 @@ extern "C" int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_
     if (int st = ctgb_unet_wgrad_chunks(n, d, h, w, &chunks)) return st;
     const int pgroups = (cin * cout + kWgThreads * kWgPairs - 1) / (kWgThreads * kWgPairs);
     const size_t smem = sizeof(float) * ((size_t)kWgSeg * cout + 3 * (size_t)(kWgSeg + 2) * cin);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(sizeof(float) * (kWgSeg * 96 + 3 * (kWgSeg + 2) * 96)));
-        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "wgrad smem attribute: %s", cudaGetErrorString(e));
-        attr = true;
-    }
     if (cin > 96 || cout > 96) return set_error(CTGB_ERR_ARG, "ctgb_unet_wgrad: at most 96 channels");
+    static std::atomic<unsigned long long> attr{0};
+    cudaError_t ea = smem_limit_once((const void *)wgrad_kernel,
+                                     (int)(sizeof(float) * (kWgSeg * 96 + 3 * (kWgSeg + 2) * 96)), attr);
+    if (ea != cudaSuccess) return set_error(CTGB_ERR_CUDA, "wgrad smem attribute: %s", cudaGetErrorString(ea));
     dim3 grid(chunks, 3, pgroups);
     wgrad_kernel<<<grid, kWgThreads, smem, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const __nv_bfloat16 *>(x), cin, static_cast<const __nv_bfloat16 *>(g), cout, partials, n, d, h,
