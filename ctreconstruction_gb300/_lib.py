@@ -61,6 +61,7 @@ SIGNATURES = {
     "ctgb_backproject_matched_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],
     "ctgb_integrate_projections": [_P, _vp, _i32, _vp, _sz, _vp],
     "ctgb_forward_launches": [_P, _i32, _i32, ctypes.POINTER(_i32)],
+    "ctgb_forward_tile_rows": [_P, ctypes.POINTER(_i32)],
     "ctgb_ray_forward": [_P, _vp, _vp, _vp, _i32, _i32, _vp],
     "ctgb_ray_backproject": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_unet_conv3d": [_vp, _i32, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp],

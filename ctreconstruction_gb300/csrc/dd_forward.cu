@@ -120,12 +120,20 @@ __global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restr
 // TMA forward projector for views whose dominant axis is x (XD) or y.
 //
 // One warp = one CTA owns a tile of kTU = 32 detector columns (one per lane) x
-// kTR = 16 rows of one view.  It walks the slices along the dominant axis; for
-// each slice the tile's footprint on the slice (a window of the volume, at
-// most kPX x kPZ voxels) is brought into shared memory by TMA boxes of
-// 64 x 1 x 8 voxels (double-buffered, one mbarrier per buffer; the next
-// slice's boxes are in flight while this slice is computed).  Out-of-volume
-// voxels arrive as zeros (TMA OOB fill), which is the reference's bounds test.
+// TR = 32 (or 16) rows of one view.  It walks the slices along the dominant
+// axis; for each slice the tile's footprint on the slice (a window of the
+// volume, at most kPX x PZ = 64 x 48 (32) voxels) is brought into shared
+// memory by TMA boxes of 64 x 1 x 8 voxels, completing on an mbarrier.
+// Out-of-volume voxels arrive as zeros (TMA OOB fill), which is the
+// reference's bounds test.
+// Tile height: the per-slice work (window, column taps, warp votes) is shared
+// by the tile's rows, so taller tiles spend less per pixel but hold more
+// accumulators and a taller patch.  At 512^3 / 720 views, 1024 x 768: 16 rows
+// (32-row patch, 24 CTAs per SM) 131.6 ms, 24 rows 129.3, 32 rows (48-row
+// patch, 16 CTAs per SM) 113.2, 40 rows 127.0, 48 rows 128.9, 64 rows 163.1.
+// At that geometry a detector row spans at most 1.18 voxel rows.  Geometries
+// whose rows span more than 1.3 voxel rows take 16-row tiles, which fit rows
+// of up to 1.75 voxel rows in their 32-row patch.
 //
 // Maths per pixel and slice (same result as the weight-calculator loop):
 //   * the column footprint [x1', x2'] and row boundaries z'_j are linear in
@@ -138,7 +146,17 @@ __global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restr
 //     so consecutive rows share their boundary term.
 // Slices whose window exceeds the patch, or whose footprint is wider than 4
 // voxels, are integrated cell by cell from global memory (compact, rare path).
-constexpr int kTU = 32, kTR = 16, kBoxX = 64, kBoxZ = 8, kPZ = 32, kPX = kBoxX;
+constexpr int kTU = 32, kBoxX = 64, kBoxZ = 8, kPX = kBoxX;
+
+// Tiles of TR = 32 or 16 detector rows.  PZ patch rows hold a tile whose rows
+// each span up to 1.3 (TR = 32) or 1.75 (TR = 16) voxel rows, with the
+// window's margins and box rounding; MINB CTAs per SM fit the registers and
+// shared memory.  The host picks TR per call (fwd_tile_rows).
+template <int TR>
+struct FwdTile {
+    static constexpr int PZ = TR == 32 ? 48 : 32;
+    static constexpr int MINB = TR == 32 ? 16 : 24;
+};
 
 // Patch buffers per CTA: 2 overlaps each slice's TMA with the previous
 // slice's compute inside the warp; 1 halves shared memory so twice as many
@@ -148,12 +166,14 @@ constexpr int kTU = 32, kTR = 16, kBoxX = 64, kBoxZ = 8, kPZ = 32, kPX = kBoxX;
 #endif
 constexpr int kFwdBufs = CTGB_FWD_BUFS;
 
+template <int TR>
 struct FwdTmaSmem {
-    float buf[kFwdBufs][kPZ][kPX];
-    float bj[kTR + 1];          // the tile's row boundaries (same for every lane)
+    float buf[kFwdBufs][FwdTile<TR>::PZ][kPX];
+    float2 bj2[TR / 2 + 1];     // (bj[j], bj[TR / 2 + j]): boundary j of both sweep chains
+    float bj[TR + 1];           // the tile's row boundaries (same for every lane)
     // per-slice row values of the fallback path; with one patch buffer they
     // live in it (no copy is in flight while a slice is computed)
-    float spill[kFwdBufs == 1 ? 1 : kTR][kTU];
+    float spill[kFwdBufs == 1 ? 1 : TR][kTU];
     uint64_t bar[2];
 };
 
@@ -185,9 +205,10 @@ struct PatchCells {
 // .y of float2 pairs, so the boundary positions, floors, fractions, cell
 // values, end terms and row sums of both chains take one packed f32x2
 // operation each (147.9 -> 137.4 ms per 512^3 / 720-view forward against
-// the scalar pair); acc2[j] holds rows j and N + j.
+// the scalar pair); acc2[j] holds rows j and N + j, and Bp[j] is boundary j
+// of both chains, (Bj[j], Bj[N + j]).
 template <int NT, bool MID, int N>
-__device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float *Bj, float A, float tau, float g,
+__device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float2 *Bp, float A, float tau, float g,
                                             float2 *acc2) {
     const float2 tau2 = make_float2(tau, tau), A2 = make_float2(A, A), g2 = make_float2(g, g);
     const float2 neg1 = make_float2(-1.0f, -1.0f), mag = make_float2(-12582912.0f, -12582912.0f);
@@ -200,50 +221,59 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float
         for (int t = 1; t < NT; ++t) h = __ffma2_rn(make_float2(pa[t], pb[t]), make_float2(o(t), o(t)), h);
         return h;
     };
-    // floor of both boundaries (round-down add of 1.5*2^23) and their fractions.
-    auto split = [&](float2 z, int &ma, int &mb, float2 &fr) {
+    // floor of both boundaries (round-down add of 1.5*2^23), the floors as
+    // floats, and the fractions.
+    auto split = [&](float2 z, int &ma, int &mb, float2 &f, float2 &fr) {
         const float2 t = __fadd2_rd(z, make_float2(12582912.0f, 12582912.0f));
         ma = __float_as_int(t.x) - 0x4B400000;
         mb = __float_as_int(t.y) - 0x4B400000;
-        const float2 f = __fadd2_rn(t, mag);                        // floor as float
+        f = __fadd2_rn(t, mag);                                     // floor as float
         fr = __ffma2_rn(f, neg1, z);                                // z - floor
     };
-    float2 z0 = __ffma2_rn(make_float2(Bj[0], Bj[N]), tau2, A2), fr0;
-    int m0a, m0b;
-    split(z0, m0a, m0b, fr0);
+    float2 z0 = __ffma2_rn(Bp[0], tau2, A2), f0, fr0;
+    int m0a, m0b;   // only addresses h0; later rows need only the float floors
+    split(z0, m0a, m0b, f0, fr0);
     float2 h0 = H2(m0a, m0b);
     float2 e0 = __fmul2_rn(h0, fr0);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        const float2 z1 = __ffma2_rn(make_float2(Bj[j + 1], Bj[N + j + 1]), tau2, A2);
+        const float2 z1 = __ffma2_rn(Bp[j + 1], tau2, A2);
         int m1a, m1b;
-        float2 fr1;
-        split(z1, m1a, m1b, fr1);
+        float2 f1, fr1;
+        split(z1, m1a, m1b, f1, fr1);
         const float2 h1 = H2(m1a, m1b);
         const float2 e1 = __fmul2_rn(h1, fr1);
-        float2 w = make_float2((m1a > m0a) ? h0.x : 0.0f, (m1b > m0b) ? h0.y : 0.0f);
+        // Cells the row crosses: d = floor(z1) - floor(z0), 0 or 1 (0, 1 or 2
+        // with MID).  Without MID the whole cell h0 enters as h0 * d, an exact
+        // product, so the row is the sum a select would give in one packed FMA
+        // (136.0 -> 132.5 ms per 512^3 / 720-view forward with the integer
+        // compares and selects).  With MID, d selects h0 and the middle cell.
+        const float2 d = __ffma2_rn(f0, neg1, f1);
+        float2 r = __ffma2_rn(e0, neg1, e1);
         if (MID) {
-            const float2 hm = H2(m0a + 1, m0b + 1);
-            w = __fadd2_rn(w, make_float2((m1a > m0a + 1) ? hm.x : 0.0f, (m1b > m0b + 1) ? hm.y : 0.0f));
+            // the middle cell of a three-cell row is m1 - 1 (read for every
+            // row; the window's one-cell margin keeps it inside the patch)
+            const float2 hm = H2(m1a - 1, m1b - 1);
+            r = __fadd2_rn(r, make_float2(d.x > 0.0f ? h0.x : 0.0f, d.y > 0.0f ? h0.y : 0.0f));
+            r = __fadd2_rn(r, make_float2(d.x > 1.0f ? hm.x : 0.0f, d.y > 1.0f ? hm.y : 0.0f));
+        } else {
+            r = __ffma2_rn(h0, d, r);
         }
-        acc2[j] = __ffma2_rn(__fadd2_rn(w, __ffma2_rn(e0, neg1, e1)), g2, acc2[j]);
-        m0a = m1a; m0b = m1b; h0 = h1; e0 = e1;
+        acc2[j] = __ffma2_rn(r, g2, acc2[j]);
+        h0 = h1; e0 = e1; f0 = f1;
     }
 }
 
-template <int NT, bool MID>
-__device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const float *Bj, float A,
+template <int NT, bool MID, int TR>
+__device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const float2 *Bp, float A,
                                            float tau, float g, float2 *acc) {
     PatchCells<NT> H;
     H.base = patch;
     H.lb = lb;
     H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
-    sweep_rows2<NT, MID, kTR / 2>(H, Bj, A, tau, g, acc);
+    sweep_rows2<NT, MID, TR / 2>(H, Bp, A, tau, g, acc);
 }
 
-#ifndef CTGB_FWD_MINB
-#define CTGB_FWD_MINB 24
-#endif
 // The views of one launch (relative to view0): every x- (or y-) dominant
 // view of the call goes into one launch, so a scan whose dominant axis
 // alternates every few views still fills the GPU with one grid per axis.
@@ -252,13 +282,14 @@ struct FwdViewList {
     int v[kFwdListViews];
 };
 
-template <bool XD, bool TMA>
-__global__ void __launch_bounds__(32, CTGB_FWD_MINB)
+template <bool XD, bool TMA, int TR>
+__global__ void __launch_bounds__(32, FwdTile<TR>::MINB)
 dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
                       const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0,
                       const __grid_constant__ FwdViewList views, int ntu, int *status) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    FwdTmaSmem &sm = *reinterpret_cast<FwdTmaSmem *>(smraw);
+    constexpr int kTR = TR, kPZ = FwdTile<TR>::PZ;
+    FwdTmaSmem<TR> &sm = *reinterpret_cast<FwdTmaSmem<TR> *>(smraw);
     const TableHeader &h = header(T);
     const int lane = threadIdx.x;
     const int vi = views.v[blockIdx.x];           // view index relative to view0
@@ -299,7 +330,11 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     float *Bj = sm.bj;
     float *spill_rows = kFwdBufs == 1 ? &sm.buf[0][0][0] : &sm.spill[0][0];
     static_assert(kTR * kTU <= kPZ * kPX, "fallback rows must fit the patch buffer");
-    if (lane <= kTR) Bj[lane] = (Sz - Bzr[min(r0 + lane, nv)]) * inv_dz;
+    for (int i = lane; i <= kTR; i += 32) Bj[i] = (Sz - Bzr[min(r0 + i, nv)]) * inv_dz;
+    __syncwarp();
+    // The sweep reads both chains' boundary j as one 8-byte load
+    // (133.5 against 135.8 ms with two 4-byte loads).
+    for (int i = lane; i <= kTR / 2; i += 32) sm.bj2[i] = make_float2(Bj[i], Bj[kTR / 2 + i]);
     __syncwarp();
     float rowspan_max = 0.0f;
 #pragma unroll
@@ -391,14 +426,14 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
                 const bool mid = __any_sync(0xffffffffu, rows_ext > 0.99f);
                 const float *patch = &sm.buf[b][0][k0 - wcur.kb];
                 if (nt == 2) {
-                    if (mid) sweep_tile<2, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
-                    else sweep_tile<2, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    if (mid) sweep_tile<2, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    else sweep_tile<2, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
                 } else if (nt == 3) {
-                    if (mid) sweep_tile<3, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
-                    else sweep_tile<3, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    if (mid) sweep_tile<3, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    else sweep_tile<3, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
                 } else {
-                    if (mid) sweep_tile<4, true>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
-                    else sweep_tile<4, false>(patch, wcur.lb, ov, Bj, A, tau, g, acc);
+                    if (mid) sweep_tile<4, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    else sweep_tile<4, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
                 }
             } else {
                 // Cell-by-cell overlap from global memory; row values go through
@@ -487,6 +522,51 @@ static void view_axes(const ctgb_params *p, int view0, int nviews, std::vector<i
     }
 }
 
+// Tile height for a scan.  At a slice the kernel's row boundaries are
+// z_j = A + B_j * tau with tau = q / D, the in-plane distances from the source
+// to the slice and to the pixel column along the pixel's ray, so a detector
+// row spans dv / dz * tau voxel rows.  D >= SDD (the detector's line or arc
+// lies at SDD from the source), and for a ray that meets the volume q is at
+// most the source's in-plane distance to the volume centre plus the volume's
+// in-plane half-diagonal.
+static int fwd_tile_rows(const ctgb_params *p) {
+    const double *S0 = p->source_init, *D0 = p->detector_init, *O = p->rotation_origin;
+    const double *C = p->flavour == CTGB_FLAVOUR_PYCUDA ? p->recon_center : p->phantom_center;
+    const double sad = std::hypot(S0[0] - O[0], S0[1] - O[1]);
+    const double sdd = std::hypot(S0[0] - D0[0], S0[1] - D0[1]);
+    if (!(sdd > 0.0) || !(p->dz > 0.0)) return 16;
+    const double q = sad + std::hypot(C[0] - O[0], C[1] - O[1]) + 0.5 * std::hypot(p->nx * p->dx, p->ny * p->dy);
+    return p->dv / p->dz * q / sdd <= 1.3 ? 32 : 16;
+}
+
+template <int TR>
+static void launch_fwd_tma(bool xd, bool tma, dim3 grid, cudaStream_t st, const CUtensorMap &tm, const float *T,
+                           const float *src, long long stk, float *d_proj, int view0, const FwdViewList &list,
+                           int ntu, int *status) {
+    const int smem = (int)sizeof(FwdTmaSmem<TR>);
+    if (xd) {
+        if (tma) dd_forward_tma_kernel<true, true, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
+        else dd_forward_tma_kernel<true, false, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
+    } else {
+        if (tma) dd_forward_tma_kernel<false, true, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
+        else dd_forward_tma_kernel<false, false, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
+    }
+}
+
+template <int TR>
+static cudaError_t fwd_smem_limits() {
+    static std::atomic<unsigned long long> attr[4];
+    const void *kernels[4] = {(const void *)dd_forward_tma_kernel<true, true, TR>,
+                              (const void *)dd_forward_tma_kernel<false, true, TR>,
+                              (const void *)dd_forward_tma_kernel<true, false, TR>,
+                              (const void *)dd_forward_tma_kernel<false, false, TR>};
+    for (int k = 0; k < 4; ++k) {
+        cudaError_t e = smem_limit_once(kernels[k], (int)sizeof(FwdTmaSmem<TR>), attr[k]);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                             float *d_proj, int32_t view0, int32_t nviews, void *stream) {
     clear_error();
@@ -517,17 +597,12 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
     if (!tma_x) std::memset(&tm_x, 0, sizeof tm_x);
     int *status = ctgb_status_ptr();
     if (!status) return set_error(CTGB_ERR_CUDA, "ctgb_forward: device status word unavailable");
-    const int smem = (int)sizeof(FwdTmaSmem);
-    static std::atomic<unsigned long long> attr[4];
-    const void *kernels[4] = {(const void *)dd_forward_tma_kernel<true, true>,
-                              (const void *)dd_forward_tma_kernel<false, true>,
-                              (const void *)dd_forward_tma_kernel<true, false>,
-                              (const void *)dd_forward_tma_kernel<false, false>};
-    for (int k = 0; k < 4; ++k) {
-        cudaError_t e = smem_limit_once(kernels[k], smem, attr[k]);
+    const int tr = fwd_tile_rows(p);
+    {
+        cudaError_t e = tr == 32 ? fwd_smem_limits<32>() : fwd_smem_limits<16>();
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "dd_forward smem attribute: %s", cudaGetErrorString(e));
     }
-    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + kTR - 1) / kTR;
+    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + tr - 1) / tr;
     const bool tiles_ok = (long long)ntu * ntv <= 65535;
     const float *src_x = d_vol_xzy ? d_vol_xzy : d_vol;
     const long long stk_x = d_vol_xzy ? 1LL : (long long)p->nx;
@@ -555,22 +630,13 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
         int n = 0;
         auto flush = [&]() {
             if (n == 0) return;
-            dim3 grid(n, ntu * ntv);
-            if (a == 0) {
-                if (tma_x)
-                    dd_forward_tma_kernel<true, true><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj, view0,
-                                                                              list, ntu, status);
-                else
-                    dd_forward_tma_kernel<true, false><<<grid, 32, smem, st>>>(tm_x, T, src_x, stk_x, d_proj, view0,
-                                                                               list, ntu, status);
-            } else {
-                if (tma_y)
-                    dd_forward_tma_kernel<false, true><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj, view0,
-                                                                               list, ntu, status);
-                else
-                    dd_forward_tma_kernel<false, false><<<grid, 32, smem, st>>>(tm_y, T, d_vol, 1, d_proj, view0,
-                                                                                list, ntu, status);
-            }
+            const dim3 grid(n, ntu * ntv);
+            const bool xd = a == 0, tma = xd ? tma_x : tma_y;
+            const CUtensorMap &tm = xd ? tm_x : tm_y;
+            const float *src = xd ? src_x : d_vol;
+            const long long stk = xd ? stk_x : 1LL;
+            if (tr == 32) launch_fwd_tma<32>(xd, tma, grid, st, tm, T, src, stk, d_proj, view0, list, ntu, status);
+            else launch_fwd_tma<16>(xd, tma, grid, st, tm, T, src, stk, d_proj, view0, list, ntu, status);
             n = 0;
         };
         for (int i = 0; i < nviews; ++i) {
@@ -583,12 +649,20 @@ extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const flo
     return check_launch("dd_forward");
 }
 
+extern "C" int ctgb_forward_tile_rows(const ctgb_params *p, int32_t *rows) {
+    clear_error();
+    if (!p || !rows) return set_error(CTGB_ERR_ARG, "ctgb_forward_tile_rows: NULL argument");
+    *rows = fwd_tile_rows(p);
+    return CTGB_OK;
+}
+
 extern "C" int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_t nviews, int32_t *launches) {
     clear_error();
     if (!p || !launches) return set_error(CTGB_ERR_ARG, "ctgb_forward_launches: NULL argument");
     if (view0 < 0 || nviews < 0 || view0 + nviews > p->nviews)
         return set_error(CTGB_ERR_ARG, "ctgb_forward_launches: view range outside [0,%d)", p->nviews);
-    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + kTR - 1) / kTR;
+    const int tr = fwd_tile_rows(p);
+    const int ntu = (p->nu + kTU - 1) / kTU, ntv = (p->nv + tr - 1) / tr;
     const bool tiles_ok = (long long)ntu * ntv <= 65535;
     std::vector<int> axes;
     view_axes(p, view0, nviews, axes);

@@ -136,6 +136,13 @@ class Projector:
         _lib.call("ctgb_forward_launches", ctypes.byref(self.c), view0, nviews, ctypes.byref(n))
         return n.value
 
+    def forward_tile_rows(self):
+        """Detector rows per tile of the forward kernel for this geometry (32,
+        or 16 where a detector row spans more than 1.3 voxel rows)."""
+        n = ctypes.c_int32(0)
+        _lib.call("ctgb_forward_tile_rows", ctypes.byref(self.c), ctypes.byref(n))
+        return n.value
+
     def integrate(self, proj, nviews=None, out=None):
         """Integrated projections of the first nviews views of proj (running
         sum along v, value) as the float2 workspace the FDK backprojector

@@ -74,6 +74,11 @@ int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, 
  * all x-dominant and one for all y-dominant views (per 2048 views), and one
  * per run of consecutive z-dominant views. */
 int ctgb_forward_launches(const ctgb_params *p, int32_t view0, int32_t nviews, int32_t *launches);
+/* Detector rows per forward tile for this scan (host-only): 32 when a
+ * detector row spans at most 1.3 voxel rows anywhere a ray meets the volume,
+ * (dv / dz) * (SAD + |centre - origin| + in-plane half-diagonal) / SDD <= 1.3,
+ * else 16.  Only speed depends on it; the projections do not. */
+int ctgb_forward_tile_rows(const ctgb_params *p, int32_t *rows);
 
 /* Same result as ctgb_forward, for callers that cannot allocate device
  * memory where they project (an application whose own pool owns the device

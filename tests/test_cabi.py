@@ -132,6 +132,26 @@ def test_product_never_imports_the_oracle():
                 assert "import oracle" not in text and "from oracle" not in text, f
 
 
+def test_forward_tile_rows():
+    """ctgb_forward_tile_rows: 32-row tiles while a detector row spans at
+    most 1.3 voxel rows where rays meet the volume, else 16 (host-only)."""
+    def rows(p):
+        c = ReconstructionParams.from_dict(p).to_ctgb()
+        n = ctypes.c_int32(0)
+        _lib.call("ctgb_forward_tile_rows", ctypes.byref(c), ctypes.byref(n))
+        return n.value
+    # (dv / dz) * (SAD + half-diagonal) / SDD: 1.5 * (100 + 17) / 150 = 1.17
+    assert rows(cone_params(n=24, dv=1.5)) == 32
+    assert rows(cone_params(n=24, dv=1.75)) == 16                      # 1.37
+    assert rows(cone_params(n=24, dv=1.5, PhantomCenter=[20.0, 0.0, 0.0])) == 16   # 1.37 off centre
+    assert rows(cone_params(n=(24, 24, 32), dv=2.0)) == 16
+    assert rows(cone_params(n=(24, 24, 24), dv=1.6)) == 32             # 1.25
+    # 512^3 at 0.5 mm, 0.75 mm rows, SAD 1000, SDD 1500: 1.18
+    big = dict(cone_params(n=512, dx=0.5, dv=0.75, nu=1024, nv=768, nviews=720),
+               SourceInit=[0.0, 1000.0, 0.0], DetectorInit=[0.0, -500.0, 0.0])
+    assert rows(big) == 32
+
+
 def test_forward_launch_count():
     """ctgb_forward_launches: a full circle from theta 0 alternates y, x, y,
     x, y dominant views, which take one launch per axis; more than 2048

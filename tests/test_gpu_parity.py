@@ -80,6 +80,10 @@ GEOMS = {
     "tma_pycuda": dict(cone_params(n=(32, 20, 14), nviews=9, nu=36, nv=24, ReconCenter=[0.5, 0.2, -0.4]),
                        DetectorOffset=[-0.7, 0.35]),
     "tma_partial_tiles": cone_params(n=(20, 28, 18), nviews=11, nu=45, nv=27),
+    # a detector row spans 0.89-1.25 voxel rows: 32-row tiles, rows over three cells
+    "tma_32row_mid": cone_params(n=(24, 24, 24), nviews=12, nu=40, nv=40, dv=1.6),
+    # 1.1-1.56 voxel rows per detector row: 16-row tiles, rows over three cells
+    "tma_16row_mid": cone_params(n=(24, 24, 32), nviews=10, nu=40, nv=20, dv=2.0),
 }
 
 
