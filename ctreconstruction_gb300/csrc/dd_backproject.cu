@@ -500,8 +500,9 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
 // ---- matched (adjoint) backprojector ---------------------------------------
 
 template <int A>
-__device__ __noinline__ float matched_voxel_view(const TableHeader &h, const float *__restrict__ T, const float *__restrict__ V,
-                                    const ViewOffsets &vo, const float *__restrict__ Q, int ix, int iy, int iz) {
+__device__ __noinline__ float matched_voxel_view(const TableHeader &h, const float *__restrict__ T,
+                                                const float *__restrict__ V, const ViewOffsets &vo,
+                                                const float *__restrict__ Q, int ix, int iy, int iz) {
     constexpr int B1 = Axes<A>::B1, B2 = Axes<A>::B2;
     const float d[3] = {h.dx, h.dy, h.dz};
     const float *planes[3] = {T + h.off_xplane, T + h.off_yplane, T + h.off_zplane};

@@ -544,13 +544,9 @@ static void launch_fwd_tma(bool xd, bool tma, dim3 grid, cudaStream_t st, const 
                            const float *src, long long stk, float *d_proj, int view0, const FwdViewList &list,
                            int ntu, int *status) {
     const int smem = (int)sizeof(FwdTmaSmem<TR>);
-    if (xd) {
-        if (tma) dd_forward_tma_kernel<true, true, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
-        else dd_forward_tma_kernel<true, false, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
-    } else {
-        if (tma) dd_forward_tma_kernel<false, true, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
-        else dd_forward_tma_kernel<false, false, TR><<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
-    }
+    auto kernel = xd ? (tma ? dd_forward_tma_kernel<true, true, TR> : dd_forward_tma_kernel<true, false, TR>)
+                     : (tma ? dd_forward_tma_kernel<false, true, TR> : dd_forward_tma_kernel<false, false, TR>);
+    kernel<<<grid, 32, smem, st>>>(tm, T, src, stk, d_proj, view0, list, ntu, status);
 }
 
 template <int TR>
