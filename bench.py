@@ -75,10 +75,10 @@ class ClockSampler:
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, tag="timed"):
         self.index = index
         self.proc = None
-        self.path = os.path.join("/tmp", "ctgb_clocks_%d_%d.csv" % (os.getpid(), index))
+        self.path = os.path.join("/tmp", "ctgb_clocks_%s_%d_%d.csv" % (tag, os.getpid(), index))
 
     def __enter__(self):
         try:
@@ -310,16 +310,18 @@ def run_ours(args):
     R.forward()
     R.backward()
     barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        R.image = pinned_vol
-        R.forward()
-        R.backward()
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    with ClockSampler(local, "e2e") as clk_e2e:
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            R.image = pinned_vol
+            R.forward()
+            R.backward()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e = {"value": ws * vv / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
            "h2d_bytes_per_step": int(4 * (n ** 3 + nviews * P.params.nu * P.params.nv)),
-           "d2h_bytes_per_step": int(4 * (n ** 3 + nviews * P.params.nu * P.params.nv))}
+           "d2h_bytes_per_step": int(4 * (n ** 3 + nviews * P.params.nu * P.params.nv)),
+           "clocks": clk_e2e.summary()}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
