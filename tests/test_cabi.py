@@ -152,6 +152,35 @@ def test_forward_tile_rows():
     assert rows(big) == 32
 
 
+@pytest.mark.parametrize("flavour", ["numba", "pycuda"])
+def test_forward_tile_rows_follows_its_bound(flavour):
+    """The tile-height choice over seeded random geometries equals
+    (dv / dz) * (SAD + |centre - origin| + in-plane half-diagonal) / SDD <= 1.3,
+    with the centre the flavour's volume centre (host-only)."""
+    rng = np.random.default_rng(7)
+    for _ in range(40):
+        sad = rng.uniform(50.0, 1200.0)
+        sdd = sad * rng.uniform(1.1, 2.5)
+        n = [int(v) for v in rng.integers(8, 600, size=3)]
+        dx = float(rng.uniform(0.2, 2.0))
+        dv = float(rng.uniform(0.2, 3.0))
+        pc = [float(v) for v in rng.uniform(-20.0, 20.0, size=3)]
+        rc = [float(v) for v in rng.uniform(-20.0, 20.0, size=3)]
+        org = [float(v) for v in rng.uniform(-5.0, 5.0, size=2)] + [0.0]
+        p = dict(cone_params(n=tuple(n), dx=dx, dv=dv), SourceInit=[org[0], org[1] + sad, 0.0],
+                 DetectorInit=[org[0], org[1] - (sdd - sad), 0.0], RotationOrigin=org, PhantomCenter=pc,
+                 ReconCenter=rc)
+        centre = rc if flavour == "pycuda" else pc
+        reach = sad + np.hypot(centre[0] - org[0], centre[1] - org[1]) + 0.5 * np.hypot(n[0] * dx, n[1] * dx)
+        ratio = dv / dx * reach / sdd
+        if abs(ratio - 1.3) < 1e-6:
+            continue
+        c = ReconstructionParams.from_dict(p, flavour).to_ctgb()
+        rows = ctypes.c_int32(0)
+        _lib.call("ctgb_forward_tile_rows", ctypes.byref(c), ctypes.byref(rows))
+        assert rows.value == (32 if ratio <= 1.3 else 16), (ratio, rows.value)
+
+
 def test_forward_launch_count():
     """ctgb_forward_launches: a full circle from theta 0 alternates y, x, y,
     x, y dominant views, which take one launch per axis; more than 2048
