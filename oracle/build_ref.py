@@ -28,7 +28,8 @@ DEFAULT_REF = "/root/reference"
 
 def extract_kernel_text(ref_root):
     path = os.path.join(ref_root, "python", "GPUFuncs_pycuda.py")
-    tree = ast.parse(open(path).read())
+    with open(path) as f:
+        tree = ast.parse(f.read())
     for node in ast.walk(tree):
         if isinstance(node, ast.Call) and getattr(node.func, "id", None) == "SourceModule":
             return node.args[0].value

@@ -17,7 +17,8 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 
 
 def declared_symbols():
-    text = open(HEADER).read()
+    with open(HEADER) as f:
+        text = f.read()
     return sorted(set(re.findall(r"\b(ctgb_\w+)\s*\(", text)))
 
 
@@ -128,7 +129,8 @@ def test_product_never_imports_the_oracle():
     for root, _, files in os.walk(pkg):
         for f in files:
             if f.endswith((".py", ".cu", ".cpp", ".h", ".cuh")):
-                text = open(os.path.join(root, f)).read()
+                with open(os.path.join(root, f)) as fh:
+                    text = fh.read()
                 assert "import oracle" not in text and "from oracle" not in text, f
 
 
