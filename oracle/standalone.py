@@ -95,7 +95,8 @@ def _lin(v, grid):
     w1, w2 = v - grid[lc], grid[hc] - v
     both = (np.abs(w1) < 1e-4) & (np.abs(w2) < 1e-4)
     w1 = np.where(both, 1.0, w1)
-    return lc, hc, w2 / (w1 + w2), w1 / (w1 + w2), ok
+    den = np.where(ok, w1 + w2, 1.0)    # samples off the grid are discarded; keep them finite
+    return lc, hc, w2 / den, w1 / den, ok
 
 
 def conebeam_backproject(p, Q):
