@@ -124,6 +124,13 @@ def test_filter_table_matches_oracle_spectrum(ft, cut):
     np.testing.assert_allclose(buf[off_h:off_h + zpl], want, rtol=2e-6, atol=1e-7 * np.abs(want).max())
 
 
+def test_integration_table_names_every_declared_symbol():
+    with open(os.path.join(os.path.dirname(HEADER), "..", "INTEGRATION.md")) as f:
+        text = f.read()
+    missing = [s for s in declared_symbols() if not re.search(r"`%s[`(]" % s, text)]
+    assert not missing, missing
+
+
 def test_product_never_imports_the_oracle():
     pkg = os.path.join(os.path.dirname(HEADER), "..", "ctreconstruction_gb300")
     for root, _, files in os.walk(pkg):
