@@ -94,7 +94,8 @@ int ctgb_forward_tile_rows(const ctgb_params *p, int32_t *rows);
 int ctgb_forward_static(const ctgb_params *p, const void *d_table, const float *d_vol, float *d_proj,
                         int32_t view0, int32_t nviews, void *stream);
 
-/* vol_xzy[z][x][y] = vol[z][y][x]. */
+/* vol_xzy[z][x][y] = vol[z][y][x]: the layout ctgb_forward reads for
+ * x-dominant views.  No reference counterpart. */
 int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t ny, int32_t nz, void *stream);
 
 /* ---- FDK-weighted DD backprojection ---------------------------------------
@@ -341,7 +342,11 @@ int ctgb_unet_colsum(const void *g, int32_t c, int64_t nvox, float *partials, in
  * error reporting). */
 #define CTGB_DEVERR_TIMEOUT 1
 int ctgb_device_status(int32_t *out, int32_t clear);
+/* The calling thread's last error message; replaces the reference's
+ * ErrorDescription printouts followed by sys.exit()
+ * (Reconstruction_numba.py:36-52). */
 const char *ctgb_last_error(void);
+/* Library version string.  No reference counterpart. */
 const char *ctgb_version(void);
 
 #ifdef __cplusplus
