@@ -938,7 +938,8 @@ using namespace ctgb;
 
 static int bp_args(const ctgb_params *p, const void *t, const float *q, float *v, int view0, int nviews,
                    const char *who) {
-    if (!p || !t || !q || !v) return set_error(CTGB_ERR_ARG, "%s: NULL argument", who);
+    // projections may be absent (an empty tensor) when no view is read
+    if (!p || !t || !v || (!q && nviews > 0)) return set_error(CTGB_ERR_ARG, "%s: NULL argument", who);
     if (view0 < 0 || nviews < 0 || view0 + nviews > p->nviews)
         return set_error(CTGB_ERR_ARG, "%s: view range [%d,%d) outside [0,%d)", who, view0, view0 + nviews,
                          p->nviews);

@@ -566,11 +566,12 @@ static cudaError_t fwd_smem_limits() {
 extern "C" int ctgb_forward(const ctgb_params *p, const void *d_table, const float *d_vol, const float *d_vol_xzy,
                             float *d_proj, int32_t view0, int32_t nviews, void *stream) {
     clear_error();
-    if (!p || !d_table || !d_vol || !d_proj) return set_error(CTGB_ERR_ARG, "ctgb_forward: NULL argument");
+    if (!p) return set_error(CTGB_ERR_ARG, "ctgb_forward: NULL argument");
     if (view0 < 0 || nviews < 0 || view0 + nviews > p->nviews)
         return set_error(CTGB_ERR_ARG, "ctgb_forward: view range [%d,%d) outside [0,%d)", view0, view0 + nviews,
                          p->nviews);
-    if (nviews == 0) return CTGB_OK;
+    if (nviews == 0) return CTGB_OK;   // nothing to read or write (an empty output has no storage)
+    if (!d_table || !d_vol || !d_proj) return set_error(CTGB_ERR_ARG, "ctgb_forward: NULL argument");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const float *T = static_cast<const float *>(d_table);
     const long long view_elems = (long long)p->nu * p->nv;

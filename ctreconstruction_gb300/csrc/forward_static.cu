@@ -51,7 +51,12 @@ static float *scratch_ptr(int *err) {
 extern "C" int ctgb_forward_static(const ctgb_params *p, const void *d_table, const float *d_vol, float *d_proj,
                                    int32_t view0, int32_t nviews, void *stream) {
     ctgb::clear_error();
-    if (!p || !d_table || !d_vol || !d_proj) return ctgb::set_error(CTGB_ERR_ARG, "ctgb_forward_static: NULL argument");
+    if (!p) return ctgb::set_error(CTGB_ERR_ARG, "ctgb_forward_static: NULL argument");
+    if (view0 < 0 || nviews < 0 || view0 + nviews > p->nviews)
+        return ctgb::set_error(CTGB_ERR_ARG, "ctgb_forward_static: view range [%d,%d) outside [0,%d)", view0,
+                               view0 + nviews, p->nviews);
+    if (nviews == 0) return CTGB_OK;
+    if (!d_table || !d_vol || !d_proj) return ctgb::set_error(CTGB_ERR_ARG, "ctgb_forward_static: NULL argument");
     if (p->nx < 1 || p->ny < 1 || p->nz < 1) return ctgb::set_error(CTGB_ERR_ARG, "ctgb_forward_static: bad volume size");
     const long long nvox = (long long)p->nx * p->ny * p->nz;
     if (nvox > (long long)CTGB_STATIC_MAX_VOXELS)

@@ -5,7 +5,10 @@
  * (NULL = legacy default stream).  No entry point allocates device memory,
  * synchronises the device or exits the process.  Every entry point returns
  * CTGB_OK or a negative status; ctgb_last_error() gives the message of the
- * calling thread's last failure.
+ * calling thread's last failure.  Projector calls take a view range
+ * [view0, view0 + nviews) inside the scan; an empty range reads no
+ * projections and writes none, so their pointers may then be NULL (a
+ * backprojection without accumulate still clears the volume).
  *
  * Array layouts follow the reference (leehoy/CTReconstruction):
  *   volume      float32 [nz][ny][nx]      (Reconstruction.image)

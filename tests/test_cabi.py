@@ -95,6 +95,25 @@ def test_table_rejects_bad_geometry():
         _lib.call("ctgb_table_build", ctypes.byref(p), small.ctypes.data_as(ctypes.c_void_p), small.nbytes)
 
 
+def test_empty_view_ranges_need_no_buffers():
+    """An empty view range is a no-op that needs no device buffers (an empty
+    tensor's data pointer is NULL); a range outside the scan is still an
+    error (host-only: nothing is launched)."""
+    p = ReconstructionParams.from_dict(cone_params(nviews=16)).to_ctgb()
+    for view0 in (0, 7, 16):
+        _lib.call("ctgb_forward", ctypes.byref(p), None, None, None, None, view0, 0, None)
+        _lib.call("ctgb_forward_static", ctypes.byref(p), None, None, None, view0, 0, None)
+    with pytest.raises(ValueError, match="view range"):
+        _lib.call("ctgb_forward", ctypes.byref(p), None, None, None, None, 17, 0, None)
+    with pytest.raises(ValueError, match="view range"):
+        _lib.call("ctgb_forward_static", ctypes.byref(p), None, None, None, -1, 0, None)
+    with pytest.raises(ValueError, match="NULL"):
+        _lib.call("ctgb_forward_static", ctypes.byref(p), None, None, None, 0, 1, None)
+    with pytest.raises(ValueError, match="NULL"):   # projections read: they must be there
+        _lib.call("ctgb_backproject_fdk", ctypes.byref(p), ctypes.c_void_p(16), None, ctypes.c_void_p(16), 0, 1,
+                  1.0, 1, None)
+
+
 def test_null_device_pointers_are_rejected_without_a_launch():
     p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
     with pytest.raises(ValueError, match="NULL"):
