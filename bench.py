@@ -60,7 +60,9 @@ def profiled_traffic(kernel):
         return None
     for f in sorted(os.listdir(d)):
         if f.startswith(kernel) and f.endswith((".md", ".txt")):
-            for line in open(os.path.join(d, f)):
+            with open(os.path.join(d, f)) as fh:
+                lines = fh.readlines()
+            for line in lines:
                 if line.strip().startswith("traffic_bytes_per_launch:"):
                     try:
                         return float(line.split(":", 1)[1].split()[0])
@@ -104,7 +106,9 @@ class ClockSampler:
             return None
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        with open(self.path) as fh:
+            lines = fh.readlines()
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
