@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "status.h"
+#include "tma.cuh"
 
 namespace ctgb {
 
@@ -31,11 +32,20 @@ constexpr int kFftThreads = 256;
 
 __device__ __forceinline__ unsigned bitrev(unsigned x, int bits) { return __brev(x) >> (32 - bits); }
 
+// zpl_launch: the row length the launch's dynamic shared memory was sized
+// for.  A table built for another length (or a malformed header) is refused:
+// the CTA sets kDevErrArg in the device status word and returns before it
+// touches shared memory or the rows.
 __global__ void __launch_bounds__(kFftThreads)
-fdk_filter_kernel(const float *__restrict__ F, float *__restrict__ proj, long long nrows) {
+fdk_filter_kernel(const float *__restrict__ F, float *__restrict__ proj, long long nrows, int zpl_launch,
+                  int *status) {
     extern __shared__ float2 sm[];
     const FilterHeaderDev &f = *reinterpret_cast<const FilterHeaderDev *>(F);
     const int N = f.zpl, bits = f.log2zpl, nu = f.nu, nv = f.nv;
+    if (N != zpl_launch || bits < 1 || bits > 13 || (1 << bits) != N || nu < 1 || nu > N || nv < 1) {
+        if (threadIdx.x == 0 && status) atomicOr(status, kDevErrArg);
+        return;
+    }
     const float *__restrict__ H = F + f.off_h;
     const float2 *__restrict__ tw = reinterpret_cast<const float2 *>(F + f.off_tw);
     const float *__restrict__ kk = F + f.off_kk;
@@ -126,7 +136,7 @@ extern "C" int ctgb_fdk_filter(const ctgb_params *p, const void *d_filter, float
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter smem: %s", cudaGetErrorString(e));
     }
     fdk_filter_kernel<<<(unsigned)nblocks, kFftThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const float *>(d_filter), d_proj, nrows);
+        static_cast<const float *>(d_filter), d_proj, nrows, zpl, ctgb_status_ptr());
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
@@ -145,7 +155,7 @@ extern "C" int ctgb_filter_apply(const void *d_filter, int32_t zpl, float *d_row
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter smem: %s", cudaGetErrorString(e));
     }
     fdk_filter_kernel<<<(unsigned)nblocks, kFftThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const float *>(d_filter), d_rows, nrows);
+        static_cast<const float *>(d_filter), d_rows, nrows, zpl, ctgb_status_ptr());
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "fdk_filter_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;

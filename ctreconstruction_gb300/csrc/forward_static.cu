@@ -18,6 +18,8 @@
 // other host threads) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "../../include/ctgb.h"
 #include "status.h"
 
@@ -25,15 +27,19 @@ namespace ctgb {
 
 static __device__ __align__(256) float g_forward_scratch[CTGB_STATIC_MAX_VOXELS];
 
+// One cached address per device ordinal.  Concurrent first calls from
+// several host threads may each look the address up; they store the same
+// value, and the atomic makes the stores and loads well defined.
 static float *scratch_ptr(int *err) {
-    static float *ptrs[64] = {nullptr};
+    static std::atomic<float *> ptrs[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= 64) {
         *err = set_error(CTGB_ERR_CUDA, "ctgb_forward_static: no current device (%s)", cudaGetErrorString(e));
         return nullptr;
     }
-    if (!ptrs[dev]) {
+    float *cached = ptrs[dev].load(std::memory_order_acquire);
+    if (!cached) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_forward_scratch);
         if (e != cudaSuccess || !p) {
@@ -41,9 +47,10 @@ static float *scratch_ptr(int *err) {
                              cudaGetErrorString(e));
             return nullptr;
         }
-        ptrs[dev] = static_cast<float *>(p);
+        cached = static_cast<float *>(p);
+        ptrs[dev].store(cached, std::memory_order_release);
     }
-    return ptrs[dev];
+    return cached;
 }
 
 }  // namespace ctgb

@@ -3,6 +3,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "status.h"
 #include "tma.cuh"
 
@@ -10,30 +12,34 @@ namespace ctgb {
 __device__ int g_device_status = 0;
 }
 
+// One cached address per device ordinal (atomic: several host threads may
+// make their first call on a device at once; all store the same value).
 int *ctgb_status_ptr() {
-    static int *ptrs[64] = {nullptr};
+    static std::atomic<int *> ptrs[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    if (!ptrs[dev]) {
+    int *cached = ptrs[dev].load(std::memory_order_acquire);
+    if (!cached) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, ctgb::g_device_status) != cudaSuccess) return nullptr;
-        ptrs[dev] = static_cast<int *>(p);
+        cached = static_cast<int *>(p);
+        ptrs[dev].store(cached, std::memory_order_release);
     }
-    return ptrs[dev];
+    return cached;
 }
 
+// The driver's tensor-map encoder, looked up once (a function-local static
+// is initialised exactly once even when several threads arrive together).
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        return nullptr;
+    }();
     return fn;
 }
 

@@ -12,6 +12,7 @@ namespace ctgb {
 
 // Status bits (CTGB_DEVERR_* in include/ctgb.h).
 constexpr int kDevErrTimeout = 1;
+constexpr int kDevErrArg = 2;       // a kernel refused a malformed device-side table
 
 constexpr long long kWaitLimit = 1LL << 26;   // ~ seconds of polling
 

@@ -199,7 +199,10 @@ int ctgb_standalone_filter_build(const ctgb_conebeam_params *p, int32_t variant,
                                  void *host_buf, size_t bytes);
 /* Filter nrows rows of length nu in place with a table from ctgb_filter_build
  * or ctgb_standalone_filter_build (rows grouped by nv rows per view for the
- * cosine weight). */
+ * cosine weight).  zpl must equal ctgb_filter_zpl() of that table: it sizes
+ * the launch's shared memory, and a kernel that finds another length in the
+ * device table leaves the rows untouched and sets CTGB_DEVERR_ARG in the
+ * device status word. */
 int ctgb_filter_apply(const void *d_filter, int32_t zpl, float *d_rows, int64_t nrows, void *stream);
 /* zpl (zero-padded row length) of a host filter table. */
 int ctgb_filter_zpl(const void *host_buf, int32_t *zpl);
@@ -339,11 +342,13 @@ int ctgb_unet_colsum(const void *g, int32_t c, int64_t nvox, float *partials, in
 
 /* ---- status ----------------------------------------------------------------
  * ctgb_device_status: the device-side status word of the current device
- * (CTGB_DEVERR_* bits set by kernels whose bounded waits ran out).  Reads it
+ * (CTGB_DEVERR_* bits set by kernels whose bounded waits ran out or that
+ * refused a malformed device-side table).  Reads it
  * with a synchronous copy (so it synchronises the device) and optionally
  * clears it.  No reference counterpart (the reference has no device-side
  * error reporting). */
 #define CTGB_DEVERR_TIMEOUT 1
+#define CTGB_DEVERR_ARG 2      /* a kernel refused a malformed device-side table */
 int ctgb_device_status(int32_t *out, int32_t clear);
 /* The calling thread's last error message; replaces the reference's
  * ErrorDescription printouts followed by sys.exit()

@@ -12,9 +12,15 @@ part of the product.  Steps:
 2. Compile that file with ``oracle/ref_launch.cpp`` into
    ``oracle/_ref/libctref.so`` with g++ and OpenMP.
 
-Where the reference checkout is absent (a machine that only received the
-working tree), step 1 is skipped and an existing ``gfp_kernels.cpp`` is
-compiled.  ``build(ref_root)`` returns the library path or None.
+The checkout's location comes from the ``ref_root`` argument or the
+``CTGB_REFERENCE_ROOT`` environment variable.  Where neither names a checkout
+(a machine that only received the working tree), step 1 is skipped and an
+existing ``gfp_kernels.cpp`` is compiled; with neither a checkout nor that
+file, ``build`` raises and says how to point it at the reference.
+``build(ref_root)`` returns the library path.
+
+    CTGB_REFERENCE_ROOT=/path/to/CTReconstruction python oracle/build_ref.py
+    python oracle/build_ref.py /path/to/CTReconstruction
 """
 import ast
 import os
@@ -23,7 +29,13 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF = "/root/reference"
+ENV_REF = "CTGB_REFERENCE_ROOT"
+
+
+def reference_root(ref_root=None):
+    """The reference checkout named by the argument or CTGB_REFERENCE_ROOT, or None."""
+    root = ref_root or os.environ.get(ENV_REF)
+    return root if root and os.path.isdir(os.path.join(root, "python")) else None
 
 
 def extract_kernel_text(ref_root):
@@ -49,12 +61,14 @@ def write_translation_unit(ref_root):
     return dst
 
 
-def build(ref_root=DEFAULT_REF, quiet=True):
+def build(ref_root=None, quiet=True):
     src = os.path.join(OUT, "gfp_kernels.cpp")
-    if os.path.isdir(os.path.join(ref_root, "python")):
-        src = write_translation_unit(ref_root)
+    root = reference_root(ref_root)
+    if root:
+        src = write_translation_unit(root)
     if not os.path.exists(src):
-        return None
+        raise RuntimeError("no reference checkout (pass its path or set %s) and no extracted %s"
+                           % (ENV_REF, os.path.relpath(src, os.path.dirname(HERE))))
     lib = os.path.join(OUT, "libctref.so")
     deps = [src, os.path.join(HERE, "ref_launch.cpp"), os.path.join(HERE, "ref_shim.h")]
     if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(d) for d in deps):
@@ -70,4 +84,4 @@ def build(ref_root=DEFAULT_REF, quiet=True):
 
 
 if __name__ == "__main__":
-    print(build(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF, quiet=False))
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None, quiet=False))

@@ -1,8 +1,8 @@
 """Generate the golden vectors in tests/golden/*.npz from the reference itself.
 
-Run in a checkout that has the reference next to it (default
-``/root/reference``); the fixtures it writes are committed, so the tests never
-need the reference at run time.
+Give the reference checkout as the first argument or in the
+``CTGB_REFERENCE_ROOT`` environment variable; the fixtures it writes are
+committed, so the tests never need the reference at run time.
 
 * numba flavour (``python/Reconstruction_numba.py`` + ``GPUFuncs_numba.py``):
   run unmodified with ``GPU: 1`` on the serial CPU stand-in for numba in
@@ -15,7 +15,8 @@ need the reference at run time.
 
 Inputs are seeded, so rerunning reproduces the files.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
+    CTGB_REFERENCE_ROOT=/path/to/reference python tests/golden/make_golden.py
 """
 import copy
 import json
@@ -204,4 +205,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CTGB_REFERENCE_ROOT")
+    if not root or not os.path.isdir(os.path.join(root, "python")):
+        sys.exit("make_golden.py: give the reference checkout as the first argument or in CTGB_REFERENCE_ROOT")
+    main(root)

@@ -123,6 +123,16 @@ def test_null_device_pointers_are_rejected_without_a_launch():
                   ctypes.c_void_p(16), 10, 100, 1.0, 0, None)
 
 
+def test_filter_apply_rejects_bad_row_lengths_without_a_launch():
+    """ctgb_filter_apply sizes its shared memory from zpl: a length that is not
+    a power of two in [2, 8192] is refused on the host (nothing launched)."""
+    fake = ctypes.c_void_p(256)
+    for zpl in (0, 1, 3, 96, 16384):
+        with pytest.raises(ValueError, match="bad arguments"):
+            _lib.call("ctgb_filter_apply", fake, zpl, fake, 4, None)
+    _lib.call("ctgb_filter_apply", fake, 64, fake, 0, None)   # no rows: no launch
+
+
 @pytest.mark.parametrize("ft,cut", [("ram-lak", 1.0), ("shepp-logan", 0.3), ("cosine", 1.0), ("hamming", 1.0),
                                     ("hann", 0.5)])
 def test_filter_table_matches_oracle_spectrum(ft, cut):

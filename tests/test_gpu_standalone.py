@@ -62,6 +62,29 @@ def test_conebeam_filter_matches_reference_loop(cuda):
     assert rel_err(q.cpu().numpy(), REF["filtered"]) < RTOL
 
 
+def test_filter_apply_refuses_a_table_of_another_length(cuda):
+    """A zpl below the table's would overrun the launch's shared memory: the
+    kernel compares the two, leaves the rows untouched and sets the
+    bad-argument bit in the device status word (the kernel's own check; no
+    out-of-bounds access happens)."""
+    from ctreconstruction_gb300.standalone import _cparams, _filter_table
+    p = dict(P, DataPath='', precision='float32')
+    c = _cparams(p)
+    table, zpl = _filter_table(c, 0, 'ram-lak', 0.3, cuda)
+    st = ctypes.c_int32(-1)
+    _lib.call("ctgb_device_status", ctypes.byref(st), 1)
+    assert st.value == 0
+    q = torch.from_numpy(np.ascontiguousarray(np.moveaxis(REF["proj"], 2, 0))).to(cuda)
+    before = q.clone()
+    _lib.call("ctgb_filter_apply", ctypes.c_void_p(table.data_ptr()), zpl // 2, ctypes.c_void_p(q.data_ptr()),
+              q.shape[0] * q.shape[1], ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.call("ctgb_device_status", ctypes.byref(st), 1)     # synchronises; clears the bit again
+    assert st.value == 2                                     # CTGB_DEVERR_ARG
+    assert torch.equal(q, before)
+    _lib.call("ctgb_device_status", ctypes.byref(st), 0)
+    assert st.value == 0
+
+
 class _Geom:
     def __init__(self, R, sdd, pw, nch, nviews, coverage=2 * math.pi):
         self.source_to_axis, self.source_to_detector, self.pixel_width = R, sdd, pw
