@@ -39,11 +39,15 @@ def headers():
 
 def _compile(src, verbose=False):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
-    newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
+    newest_dep = max([os.path.getmtime(src), os.path.getmtime(os.path.abspath(__file__))] +
+                     [os.path.getmtime(h) for h in headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep:
         return obj
-    cmd = [_nvcc(), "-c", src, "-o", obj, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
-           "-lineinfo"]
+    # -ffp-contract=off: host arithmetic (the geometry tables, the dominant-axis
+    # choice, whose ties the reference's NumPy breaks without fused
+    # multiply-adds) rounds the same on x86-64 and aarch64 hosts.
+    cmd = [_nvcc(), "-c", src, "-o", obj, "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "-I", INCLUDE, "-I", CSRC, "-lineinfo"]
     if src.endswith(".cu"):
         cmd += ARCH + ["-Xptxas", "-v" if verbose else "-O3"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -70,10 +70,12 @@ def build(ref_root=None, quiet=True):
         raise RuntimeError("no reference checkout (pass its path or set %s) and no extracted %s"
                            % (ENV_REF, os.path.relpath(src, os.path.dirname(HERE))))
     lib = os.path.join(OUT, "libctref.so")
-    deps = [src, os.path.join(HERE, "ref_launch.cpp"), os.path.join(HERE, "ref_shim.h")]
+    deps = [src, os.path.join(HERE, "ref_launch.cpp"), os.path.join(HERE, "ref_shim.h"), os.path.abspath(__file__)]
     if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(d) for d in deps):
         return lib
-    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-shared", "-fPIC", "-w", "-o", lib, src,
+    # -ffp-contract=off: the rounding the golden vectors were made with (an
+    # x86-64 host, no fused multiply-adds), also on aarch64 hosts.
+    cmd = ["g++", "-O2", "-ffp-contract=off", "-std=c++17", "-fopenmp", "-shared", "-fPIC", "-w", "-o", lib, src,
            os.path.join(HERE, "ref_launch.cpp")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

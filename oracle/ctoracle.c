@@ -124,7 +124,7 @@ static fwd_view fwd_setup(const ct_geom *g, double th) {
 typedef void (*visit_fn)(void *ctx, long vox, double w);
 
 static void pixel_footprint(const ct_geom *g, const fwd_view *f, double th, int r, int c,
-                            const double *plane[3], const double d[3], const int n[3],
+                            const double *plane[3], const double d[3], const int n[3], int is0, int is1,
                             visit_fn visit, void *ctx) {
     const double *S = f->S;
     double PU1[3], PU2[3], PC[3], B1[3], B2[3];
@@ -154,7 +154,8 @@ static void pixel_footprint(const ct_geom *g, const fwd_view *f, double th, int 
     double t1 = (S[b1] - PC[b1]) / (S[a] - PC[a]), t2 = (S[b2] - PC[b2]) / (S[a] - PC[a]);
     double L = fabs(d[a]) / (cos(atan(t1)) * cos(atan(t2)));
     double eps = g->eps_fwd;
-    for (int is = 0; is < n[a]; ++is) {
+    /* Slices [is0, is1) of the dominant axis (all of them for the forward). */
+    for (int is = is0; is < is1; ++is) {
         double pc = plane[a][is] + d[a] / 2.0;
         double c11 = sU1 * pc + iU1, c12 = sU2 * pc + iU2;
         double c21 = sV1 * pc + iV1, c22 = sV2 * pc + iV2;
@@ -213,15 +214,18 @@ void ct_forward(const ct_geom *g, const double *angles, int view0, int nview, co
         int r = (int)((t % npix) / g->nu), c = (int)(t % g->nu);
         fwd_view f = fwd_setup(g, angles[v]);
         gather_ctx ctx = {vol, 0.0};
-        pixel_footprint(g, &f, angles[v], r, c, plane, d, n, gather_visit, &ctx);
+        pixel_footprint(g, &f, angles[v], r, c, plane, d, n, 0, n[f.axis], gather_visit, &ctx);
         proj[t] = ctx.acc;
     }
     free(xp); free(yp); free(zp);
 }
 
-/* vol += A^T proj over views [view0, view0+nview) (serial; exact transpose). */
+/* vol += A^T proj over views [view0, view0+nview): the exact transpose of
+ * ct_forward.  Within a view every pixel's footprint on slice `is` of the
+ * dominant axis touches only voxels of that slice, so threads own disjoint
+ * slice ranges and scatter without races. */
 void ct_backproject_matched(const ct_geom *g, const double *angles, int view0, int nview, const float *proj,
-                            double *vol) {
+                            double *vol, int nthreads) {
     double *xp = malloc(sizeof(double) * (g->nx + 1)), *yp = malloc(sizeof(double) * (g->ny + 1)),
            *zp = malloc(sizeof(double) * (g->nz + 1));
     double d[3];
@@ -231,10 +235,20 @@ void ct_backproject_matched(const ct_geom *g, const double *angles, int view0, i
     long npix = (long)g->nu * g->nv;
     for (int v = view0; v < view0 + nview; ++v) {
         fwd_view f = fwd_setup(g, angles[v]);
-        for (long p = 0; p < npix; ++p) {
-            scatter_ctx ctx = {vol, (double)proj[(long)(v - view0) * npix + p]};
-            if (ctx.val == 0.0) continue;
-            pixel_footprint(g, &f, angles[v], (int)(p / g->nu), (int)(p % g->nu), plane, d, n, scatter_visit, &ctx);
+        const int ns = n[f.axis];
+        /* A few slice ranges per thread: each range repeats the pixels'
+         * per-view set-up, so more ranges cost more. */
+        const int want = 4 * (nthreads > 0 ? nthreads : 1);
+        const int nchunk = ns < want ? ns : want;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+        for (int k = 0; k < nchunk; ++k) {
+            const int is0 = (int)((long)ns * k / nchunk), is1 = (int)((long)ns * (k + 1) / nchunk);
+            for (long p = 0; p < npix; ++p) {
+                scatter_ctx ctx = {vol, (double)proj[(long)(v - view0) * npix + p]};
+                if (ctx.val == 0.0) continue;
+                pixel_footprint(g, &f, angles[v], (int)(p / g->nu), (int)(p % g->nu), plane, d, n, is0, is1,
+                                scatter_visit, &ctx);
+            }
         }
     }
     free(xp); free(yp); free(zp);

@@ -37,9 +37,13 @@ def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "ctoracle.c")
     lib = os.path.join(BUILD, "libctoracle.so")
-    if force or not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
-        subprocess.run(["gcc", "-O2", "-fopenmp", "-shared", "-fPIC", "-std=c11", "-D_DEFAULT_SOURCE",
-                        "-o", lib, src, "-lm"], check=True)
+    newest = max(os.path.getmtime(src), os.path.getmtime(os.path.abspath(__file__)))
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        # -ffp-contract=off: the same rounding as NumPy (no fused multiply-adds)
+        # on every host, so exact ties (a 45-degree view's dominant axis) break
+        # the way the reference's NumPy breaks them.
+        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", "-std=c11",
+                        "-D_DEFAULT_SOURCE", "-o", lib, src, "-lm"], check=True)
     return lib
 
 
@@ -51,7 +55,7 @@ def lib():
         _LIB.ct_forward.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
                                     P(ctypes.c_float), P(ctypes.c_double), ctypes.c_int]
         _LIB.ct_backproject_matched.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
-                                                P(ctypes.c_float), P(ctypes.c_double)]
+                                                P(ctypes.c_float), P(ctypes.c_double), ctypes.c_int]
         _LIB.ct_backproject_fdk.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, P(ctypes.c_float), P(ctypes.c_double), ctypes.c_int]
         _LIB.ct_ray_forward.argtypes = [P(CtGeom), P(ctypes.c_double), ctypes.c_int, ctypes.c_int,
@@ -134,11 +138,12 @@ class OracleGeometry:
                                  nthreads or os.cpu_count())
         return out
 
-    def backward_matched(self, proj, view0=0, nview=None):
+    def backward_matched(self, proj, view0=0, nview=None, nthreads=0):
         nview = self.nviews - view0 if nview is None else nview
         q = np.ascontiguousarray(proj, dtype=np.float32).reshape(nview, self.nv, self.nu)
         out = np.zeros((self.nz, self.ny, self.nx), dtype=np.float64)
-        lib().ct_backproject_matched(ctypes.byref(self.g), _dp(self.angles), view0, nview, _fp(q), _dp(out))
+        lib().ct_backproject_matched(ctypes.byref(self.g), _dp(self.angles), view0, nview, _fp(q), _dp(out),
+                                     nthreads or os.cpu_count())
         return out
 
     def ray_forward(self, image, view0=0, nview=None, nthreads=0):

@@ -51,3 +51,25 @@ def cone_params(n=24, nviews=16, nu=40, nv=32, du=1.0, dv=1.0, dx=1.0, start=0.0
          'Pitch': 0.0}
     p.update(kw)
     return p
+
+
+def cfg3_params(**kw):
+    """The DD-pair benchmark scan: 512^3 at 0.5 mm, 720 views over 2 pi,
+    1024x768 detector at 0.75 mm, SAD 1000 mm, SDD 1500 mm."""
+    p = {'SourceInit': [0.0, 1000.0, 0.0], 'DetectorInit': [0.0, -500.0, 0.0], 'StartAngle': 0.0,
+         'EndAngle': 2 * np.pi, 'NumberOfDetectorPixels': [1024, 768], 'DetectorPixelSize': [0.75, 0.75],
+         'NumberOfViews': 720, 'ImagePixelSpacing': [0.5, 0.5, 0.5], 'NumberOfImage': [512, 512, 512],
+         'PhantomCenter': [0.0, 0.0, 0.0], 'RotationOrigin': [0.0, 0.0, 0.0], 'ReconCenter': [0.0, 0.0, 0.0],
+         'Method': 'Distance', 'FilterType': 'hann', 'cutoff': 1.0, 'GPU': 1, 'DetectorShape': 'Flat',
+         'Pitch': 0.0}
+    p.update(kw)
+    return p
+
+
+def cfg1_params(**kw):
+    """The FDK benchmark scan: 128^3 at 1 mm, 360 views over 2 pi, 256x192
+    detector at 1.5 mm, SAD 1000 mm, SDD 1500 mm, Hann ramp."""
+    p = cfg3_params(NumberOfDetectorPixels=[256, 192], DetectorPixelSize=[1.5, 1.5], NumberOfViews=360,
+                    ImagePixelSpacing=[1.0, 1.0, 1.0], NumberOfImage=[128, 128, 128])
+    p.update(kw)
+    return p

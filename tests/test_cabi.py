@@ -82,6 +82,30 @@ def test_geometry_table_matches_oracle_geometry(name, flavour):
         assert int(rec[0]) == want
 
 
+def test_dominant_axis_ties_break_like_the_reference():
+    """At 720 views over 2 pi, views 90, 270, 450 and 630 sit at 45 degrees,
+    where |S_x - D_x| and |S_y - D_y| agree to the last bit or two.  The
+    table's axis must follow distance_forward's test
+    (Reconstruction_numba.py:896,966) evaluated as the reference evaluates it:
+    math.sin/cos, NumPy float64 products and differences, no fused
+    multiply-adds."""
+    import math
+    from _util import cfg3_params
+    p = cfg3_params(NumberOfImage=[8, 8, 8], NumberOfDetectorPixels=[8, 8])
+    buf = _table(p)
+    h = _header(buf)
+    SAD, SDD = 1000.0, 1500.0
+    angles = np.linspace(0.0, 2 * np.pi, 721)[:-1]
+    ties = 0
+    for v, th in enumerate(angles):
+        S = np.array([-SAD * math.sin(th), SAD * math.cos(th)])
+        D = np.array([(SDD - SAD) * math.sin(th), -(SDD - SAD) * math.cos(th)])
+        ax, ay = abs(S[0] - D[0]), abs(S[1] - D[1])
+        ties += ax == ay
+        assert int(buf[h["off_views"] + v * h["view_stride"]]) == (0 if ax >= ay else 1), v
+    assert ties >= 1
+
+
 def test_table_rejects_bad_geometry():
     p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
     p.nu = 0
