@@ -37,6 +37,10 @@ enum ViewField {
     VF_ANGLE,
     VF_EUX, VF_EUY,               // detector u axis (cos, sin)
     VF_EWX, VF_EWY,               // detector normal (sin, -cos)
+    // Detector-row boundaries in the forward projector's z units:
+    // B(r) = (S_z - Bz[r]) / dz (dz signed) = VF_B0 + r * VF_DB exactly for
+    // the uniform rows of every supported detector; both from float64.
+    VF_B0, VF_DB,
     kViewScalars = 16
 };
 // Column/row tables inside a view record (offsets in floats from the record start):

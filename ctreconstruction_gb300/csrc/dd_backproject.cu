@@ -604,11 +604,11 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
         const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
         const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
         const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
-        const float *__restrict__ Bzr = V + vo.bz;
         const float *__restrict__ Pzr = V + vo.pz;
         const float inv_db = 1.0f / db;
         const float Cb = (Sb - pb[0]) * inv_db;
         const float A = (Sz - pzp[0]) * inv_dz;
+        const float B0 = V[VF_B0], dB = V[VF_DB];
         const float q = pa[s] + 0.5f * da - Sa;
         const float g = 1.0f / (q * q);
         // Candidate columns: project the voxel's b1 edges on the slice centre plane.
@@ -638,23 +638,20 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
             const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
             const float vscale = ovx * g * base;
             // First row whose lower boundary lies above voxel boundary l0.
-            int r = 0;
-            {
-                const float B0 = (Sz - Bzr[0]) * inv_dz, B1 = (Sz - Bzr[1]) * inv_dz;
-                const float est = (((float)l0 - A) / tau - B0) / (B1 - B0);
-                r = min(max((int)floorf(est) - 1, 0), nv);
-            }
+            const int rs = min(max((int)floorf(((float)l0 - A) / (tau * dB) - B0 / dB) - 1, 0), nv);
+            // Rows rs + i in the frame of row rs (local z: the frame's integer
+            // part removed), placed as the forward places them.
+            const ZFrame zf = row_frame(A, tau, B0, dB, (float)rs);
+            int r = rs, i = 0;
             // Row r spans [zr, zr1]; C = running integral up to zr.
-            float Bcur = (Sz - Bzr[r]) * inv_dz;
-            float zr = fmaf(Bcur, tau, A);
-            float C = 0.0f, vr = 0.0f, zr1 = zr, Bnext = Bcur;
+            float zr = zf.f;
+            float C = 0.0f, vr = 0.0f, zr1 = zr;
             bool have_row = false;
             auto load_row = [&]() {
                 if (r < nv) {
-                    Bnext = (Sz - Bzr[r + 1]) * inv_dz;
-                    zr1 = fmaf(Bnext, tau, A);
+                    zr1 = fmaf((float)(i + 1), zf.sg, zf.f);
                     const float t2 = (Sz - Pzr[r]) * invD;
-                    const float K = sqrtf(1.0f + t2 * t2) / fabsf(Bnext - Bcur);
+                    const float K = sqrtf(1.0f + t2 * t2) / fabsf(dB);
                     vr = __ldg(Q + (long long)r * nu + c) * K * vscale;
                     have_row = true;
                 } else {
@@ -666,13 +663,13 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
             float Rprev = 0.0f;
 #pragma unroll
             for (int j = 0; j <= kMZ; ++j) {
-                const float lb = (float)(l0 + j);
+                const float lb = (float)(l0 + j) - zf.ibf;   // voxel boundary, local z
                 // Advance past rows that end at or below this voxel boundary.
                 while (have_row && zr1 <= lb) {
                     C += vr * (zr1 - zr);
                     zr = zr1;
-                    Bcur = Bnext;
                     ++r;
+                    ++i;
                     load_row();
                 }
                 const float Rb = C + ((have_row && lb > zr) ? vr * (lb - zr) : 0.0f);
@@ -732,10 +729,9 @@ __global__ void matched_integrate_kernel(const float *__restrict__ T, const floa
     const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
     const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
     const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
-    const float *__restrict__ Bzr = V + vo.bz;
     const float *__restrict__ Pzr = V + vo.pz;
     const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
-    const float inv_db = 1.0f / db, inv_dz = 1.0f / h.dz;
+    const float inv_db = 1.0f / db;
     // The forward's per-pixel factor (dd_forward_tma_kernel epilogue), same expressions.
     const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
     const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
@@ -746,15 +742,13 @@ __global__ void matched_integrate_kernel(const float *__restrict__ T, const floa
     tab[nu + 1 + c] = invD;
     const float t1 = (Sb - Pb[c]) * invD;
     const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
-    float Bprev = (Sz - Bzr[0]) * inv_dz;
+    const float rowspan = fabsf(V[VF_DB]);
     for (int r = 0; r < nv; ++r) {
-        const float Bnext = (Sz - Bzr[r + 1]) * inv_dz;
         const float t2 = (Sz - Pzr[r]) * invD;
-        const float K = base * sqrtf(1.0f + t2 * t2) / fabsf(Bnext - Bprev);
+        const float K = base * sqrtf(1.0f + t2 * t2) / rowspan;
         const float y = __ldg(q + (long long)r * nu) * K;
         o[(long long)r * nu] = make_float2((float)run, y);
         run += y;
-        Bprev = Bnext;
     }
     o[(long long)nv * nu] = make_float2((float)run, 0.0f);
 }
@@ -814,14 +808,12 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         const float *__restrict__ pb = T + (xd ? h.off_yplane : h.off_xplane);
         const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
         const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
-        const float *__restrict__ Bzr = V + vo.bz;
         const float inv_db = 1.0f / db;
         const float Cb = (Sb - pb[0]) * inv_db;
         const float A = (Sz - pzp[0]) * inv_dz;
         const float q = pa[s] + 0.5f * da - Sa;
         const float g = 1.0f / (q * q);
-        const float B0 = (Sz - Bzr[0]) * inv_dz;
-        const float dB = ((Sz - Bzr[nv]) * inv_dz - B0) / fnv;       // row pitch of B
+        const float B0 = V[VF_B0], dB = V[VF_DB];                     // row boundary r: B0 + r dB
         // Candidate columns: project the voxel's transverse edges on the slice centre plane.
         float cmin = INFINITY, cmax = -INFINITY;
 #pragma unroll
@@ -842,9 +834,9 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         const float *__restrict__ IPT = EbT + nu + 1;
         int ncol = 0;
         int cc[kMC];
-        float wcol[kMC], al[kMC], be[kMC];
+        float wcol[kMC], tw[kMC], be[kMC];
 #pragma unroll
-        for (int m = 0; m < kMC; ++m) { cc[m] = 0; wcol[m] = 0.0f; al[m] = 0.0f; be[m] = 0.0f; }
+        for (int m = 0; m < kMC; ++m) { cc[m] = 0; wcol[m] = 0.0f; tw[m] = 0.0f; be[m] = 0.0f; }
         bool overflow = false;
         for (int c = cA; c <= cB; ++c) {
             const float Eb0 = __ldg(EbT + c), Eb1 = __ldg(EbT + c + 1);
@@ -858,7 +850,7 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             if (ncol < kMC) {
 #pragma unroll
                 for (int m = 0; m < kMC; ++m)
-                    if (m == ncol) { cc[m] = c; wcol[m] = ovx * g * wz; al[m] = (-A / tau - B0) / dB; be[m] = inv; }
+                    if (m == ncol) { cc[m] = c; wcol[m] = ovx * g * wz; tw[m] = tau; be[m] = inv; }
                 ++ncol;
             } else {
                 overflow = true;
@@ -876,24 +868,33 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             continue;
         }
         if (!live) continue;
-        // Voxel j spans row coordinates [r_j, r_{j+1}] (r_j = al + (l0 + j) be):
-        // consecutive voxels share a boundary, so each of the kMZ + 1
-        // boundaries is clamped to [0, nv] and looked up once, and voxel j
-        // takes e(r_{j+1}) - e(r_j) with e(r) = C + frac * y', signed by the
-        // orientation of be.
+        // Voxel j spans row coordinates [r_j, r_{j+1}]: consecutive voxels
+        // share a boundary, so each of the kMZ + 1 boundaries is clamped to
+        // [0, nv] and looked up once, and voxel j takes e(r_{j+1}) - e(r_j)
+        // with e(r) = C + frac * y', signed by the orientation of be.  The
+        // row coordinate of boundary l is found in the frame of row R near
+        // the chunk (row_frame: the forward's row placement, exact to ~1e-6
+        // voxel): r = R + ((l - ibf) - f) / (tau dB), so rows are placed as
+        // the forward places them and the weights agree to float rounding
+        // of small local coordinates.
+        const float b0r = B0 / dB;
 #pragma unroll
         for (int m = 0; m < kMC; ++m) {
             if (m >= ncol) break;
             const float2 *__restrict__ colp = IQ + cc[m];
             const float w = be[m] > 0.0f ? wcol[m] : -wcol[m];
+            const int R = min(max((int)floorf(fmaf((float)l0 - A, be[m], -b0r)), 0), nv);
+            const ZFrame zf = row_frame(A, tw[m], B0, dB, (float)R);
+            const float d0 = ((float)l0 - zf.ibf) - zf.f;                 // local z of boundary l0
+            const float rlo = -(float)R, rhi = fnv - (float)R;          // rows 0 and nv, relative to R
             float eprev = 0.0f;
 #pragma unroll
             for (int j = 0; j <= kMZ; ++j) {
-                const float r = fminf(fmaxf(fmaf((float)(l0 + j), be[m], al[m]), 0.0f), fnv);
+                const float rr = fminf(fmaxf((d0 + (float)j) * be[m], rlo), rhi);   // rows past R
                 float fr;
-                const int mr = floor_split(r, &fr);
+                const int mr = R + floor_split(rr, &fr);
                 const float2 a = __ldg(colp + (long long)mr * nu);
-                const float e = fmaf(a.y, r - fr, a.x);
+                const float e = fmaf(a.y, rr - fr, a.x);
                 if (j > 0) acc[j - 1] = fmaf(e - eprev, w, acc[j - 1]);
                 eprev = e;
             }

@@ -55,6 +55,46 @@ __device__ __forceinline__ PixelLines pixel_lines(const float *__restrict__ V, c
     return L;
 }
 
+// Detector-row boundaries on one slice of an x/y-dominant view, in voxel
+// units along z.  Row boundary r of the column whose ray factor is tau meets
+// the slice at
+//     Z(r) = A + tau * (B0 + r * dB),   A = (S_z - zplane_0) / dz,
+// (B0, dB from the view record).  In float32 a position near z index 512
+// carries up to 3e-5 voxel of rounding, which is 3e-5 of a row's weight: the
+// forward projector and its matched adjoint would each be that far from the
+// exact weights, and from each other.  So both evaluate Z from the same float
+// inputs as if in exact arithmetic: Z at a base row R as an unevaluated sum
+// (integer part + small remainder) by error-free products and sums, and rows
+// R + j near it as remainder + j * tau * dB in plain float (|value| < 64, so
+// below 4e-6 voxel of rounding).  The intrinsics keep the compiler from
+// fusing the products that the error terms recover.
+struct ZFrame {
+    float ibf;   // integer part of Z(R), as a float
+    float f;     // Z(R) - ibf (small; may be slightly negative)
+    float sg;    // tau * dB, the local step per row
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ ZFrame row_frame(float A, float tau, float B0, float dB, float R) {
+    const float p1 = __fmul_rn(tau, B0), e1 = fmaf(tau, B0, -p1);    // tau B0 = p1 + e1
+    const float sg = __fmul_rn(tau, dB), es = fmaf(tau, dB, -sg);    // tau dB = sg + es
+    const float p2 = __fmul_rn(R, sg), e2 = fmaf(R, sg, -p2);        // R sg = p2 + e2
+    float s1, t1, s2, t2;
+    two_sum(A, p1, s1, t1);
+    two_sum(s1, p2, s2, t2);
+    const float lo = fmaf(R, es, __fadd_rn(__fadd_rn(t1, t2), __fadd_rn(e1, e2)));
+    ZFrame z;
+    z.ibf = floorf(s2);
+    z.f = __fadd_rn(__fsub_rn(s2, z.ibf), lo);
+    z.sg = sg;
+    return z;
+}
+
 // One axis of a pixel footprint on one slice: the covered cell range and the
 // quantities weight_calculator1/2 (python/GPUFuncs_numba.py:16-47) need.
 struct Span {

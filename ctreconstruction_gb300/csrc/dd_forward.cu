@@ -169,8 +169,6 @@ constexpr int kFwdBufs = CTGB_FWD_BUFS;
 template <int TR>
 struct FwdTmaSmem {
     float buf[kFwdBufs][FwdTile<TR>::PZ][kPX];
-    float2 bj2[TR / 2 + 1];     // (bj[j], bj[TR / 2 + j]): boundary j of both sweep chains
-    float bj[TR + 1];           // the tile's row boundaries (same for every lane)
     // per-slice row values of the fallback path; with one patch buffer they
     // live in it (no copy is in flight while a slice is computed)
     float spill[kFwdBufs == 1 ? 1 : TR][kTU];
@@ -180,13 +178,15 @@ struct FwdTmaSmem {
 struct TileWindow {
     int kb, lb, nbz;     // patch origin (kb multiple of 4) and number of 8-row boxes
     bool active, fits;
+    ZFrame zf;           // the lane's row boundaries on the slice: tile row j at zf.ibf + zf.f + j * zf.sg
 };
 
-// h(m): the lane's column footprint (NT taps) applied to patch row m.
+// h(m): the lane's column footprint (NT taps) applied to the patch row of
+// local cell m (z index m + frame integer part).
 template <int NT>
 struct PatchCells {
     const float *base;   // &patch[0][k0 - kb]
-    int lb;
+    int lb;              // window base minus the frame's integer part
     float ov0, ov1, ov2, ov3;
     __device__ __forceinline__ float operator()(int m) const {
         const float *p = base + (m - lb) * kPX;
@@ -205,12 +205,12 @@ struct PatchCells {
 // .y of float2 pairs, so the boundary positions, floors, fractions, cell
 // values, end terms and row sums of both chains take one packed f32x2
 // operation each (147.9 -> 137.4 ms per 512^3 / 720-view forward against
-// the scalar pair); acc2[j] holds rows j and N + j, and Bp[j] is boundary j
-// of both chains, (Bj[j], Bj[N + j]).
+// the scalar pair); acc2[j] holds rows j and N + j.  Boundary j of the tile
+// sits at local z f + j * sg (the frame of row_frame; cells are local too,
+// PatchCells adds the frame's integer part).
 template <int NT, bool MID, int N>
-__device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float2 *Bp, float A, float tau, float g,
-                                            float2 *acc2) {
-    const float2 tau2 = make_float2(tau, tau), A2 = make_float2(A, A), g2 = make_float2(g, g);
+__device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, float f, float sg, float g, float2 *acc2) {
+    const float2 sg2 = make_float2(sg, sg), f2 = make_float2(f, f), g2 = make_float2(g, g);
     const float2 neg1 = make_float2(-1.0f, -1.0f), mag = make_float2(-12582912.0f, -12582912.0f);
     auto o = [&](int t) { return t == 0 ? H.ov0 : (t == 1 ? H.ov1 : (t == 2 ? H.ov2 : H.ov3)); };
     // h for both chains: NT cells of each chain's row, weighted by the column footprint.
@@ -230,14 +230,14 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float
         f = __fadd2_rn(t, mag);                                     // floor as float
         fr = __ffma2_rn(f, neg1, z);                                // z - floor
     };
-    float2 z0 = __ffma2_rn(Bp[0], tau2, A2), f0, fr0;
+    float2 z0 = __ffma2_rn(make_float2(0.0f, (float)N), sg2, f2), f0, fr0;
     int m0a, m0b;   // only addresses h0; later rows need only the float floors
     split(z0, m0a, m0b, f0, fr0);
     float2 h0 = H2(m0a, m0b);
     float2 e0 = __fmul2_rn(h0, fr0);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        const float2 z1 = __ffma2_rn(Bp[j + 1], tau2, A2);
+        const float2 z1 = __ffma2_rn(make_float2((float)(j + 1), (float)(N + j + 1)), sg2, f2);
         int m1a, m1b;
         float2 f1, fr1;
         split(z1, m1a, m1b, f1, fr1);
@@ -265,13 +265,13 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, const float
 }
 
 template <int NT, bool MID, int TR>
-__device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const float2 *Bp, float A,
-                                           float tau, float g, float2 *acc) {
+__device__ __forceinline__ void sweep_tile(const float *patch, int lb, const float *ov, const ZFrame &zf, float g,
+                                           float2 *acc) {
     PatchCells<NT> H;
     H.base = patch;
-    H.lb = lb;
+    H.lb = lb - (int)zf.ibf;
     H.ov0 = ov[0]; H.ov1 = ov[1]; H.ov2 = ov[2]; H.ov3 = ov[3];
-    sweep_rows2<NT, MID, TR / 2>(H, Bp, A, tau, g, acc);
+    sweep_rows2<NT, MID, TR / 2>(H, zf.f, zf.sg, g, acc);
 }
 
 // The views of one launch (relative to view0): every x- (or y-) dominant
@@ -313,7 +313,6 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     const float *__restrict__ Bb = V + (XD ? vo.by : vo.bx);
     const float *__restrict__ Pa = V + (XD ? vo.px : vo.py);
     const float *__restrict__ Pb = V + (XD ? vo.py : vo.px);
-    const float *__restrict__ Bzr = V + vo.bz;
     const float *__restrict__ Pzr = V + vo.pz;
 
     // Column constants (lanes beyond nu use the last column and do not write).
@@ -325,20 +324,11 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
     const float invD = 1.0f / (Sa - Pa[cc]);
     const float t1 = (Sb - Pb[cc]) * invD;
     const float A = (Sz - pzp[0]) * inv_dz;
-    // Row boundaries in shared memory: one copy per warp instead of kTR + 1
-    // registers per lane (broadcast reads).
-    float *Bj = sm.bj;
+    // Row boundaries: B(r) = B0 + r dB (uniform rows), placed on each slice by
+    // row_frame from the tile's first row.
+    const float B0 = V[VF_B0], dB = V[VF_DB], rowspan_max = fabsf(dB);
     float *spill_rows = kFwdBufs == 1 ? &sm.buf[0][0][0] : &sm.spill[0][0];
     static_assert(kTR * kTU <= kPZ * kPX, "fallback rows must fit the patch buffer");
-    for (int i = lane; i <= kTR; i += 32) Bj[i] = (Sz - Bzr[min(r0 + i, nv)]) * inv_dz;
-    __syncwarp();
-    // The sweep reads both chains' boundary j as one 8-byte load
-    // (133.5 against 135.8 ms with two 4-byte loads).
-    for (int i = lane; i <= kTR / 2; i += 32) sm.bj2[i] = make_float2(Bj[i], Bj[kTR / 2 + i]);
-    __syncwarp();
-    float rowspan_max = 0.0f;
-#pragma unroll
-    for (int j = 0; j < kTR; ++j) rowspan_max = fmaxf(rowspan_max, fabsf(Bj[j + 1] - Bj[j]));
 
     // Per-slice tile window: the union of every lane's exact footprint cells
     // (the same expressions the sweep evaluates, so every cell the sweep
@@ -348,11 +338,13 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         const float q = pa[s] + 0.5f * da - Sa;
         const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
         const float tau = q * invD;
-        const float za = fmaf(Bj[0], tau, A), zb = fmaf(Bj[kTR], tau, A);
+        w.zf = row_frame(A, tau, B0, dB, (float)r0);
+        const float za = w.zf.f, zb = fmaf((float)kTR, w.zf.sg, w.zf.f);   // local z of boundaries 0, kTR
+        const int ib = (int)w.zf.ibf;
         const int klo = __reduce_min_sync(0xffffffffu, (int)floorf(fminf(xa, xb))) - 1;
         const int khi = __reduce_max_sync(0xffffffffu, (int)floorf(fmaxf(xa, xb))) + 1;
-        const int llo = __reduce_min_sync(0xffffffffu, (int)floorf(fminf(za, zb))) - 1;
-        const int lhi = __reduce_max_sync(0xffffffffu, (int)floorf(fmaxf(za, zb))) + 1;
+        const int llo = __reduce_min_sync(0xffffffffu, ib + (int)floorf(fminf(za, zb))) - 1;
+        const int lhi = __reduce_max_sync(0xffffffffu, ib + (int)floorf(fmaxf(za, zb))) + 1;
         w.active = !(khi < 0 || klo >= nB || lhi < 0 || llo >= nZ);
         w.kb = (klo >= 0 ? klo : klo - 3) / 4 * 4;           // floor to a multiple of 4
         w.lb = llo;
@@ -408,11 +400,10 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
             const float g = 1.0f / (q * q);
             const float xa = fmaf(Eb0, q, Cb), xb = fmaf(Eb1, q, Cb);
             const float lo = fminf(xa, xb), hi = fmaxf(xa, xb);
-            const float tau = q * invD;
             float fk;
             const int k0 = floor_split(lo, &fk);
-            // Row extent in cells: |B_{j+1} - B_j| * |tau|, at most rowspan_max * |tau|.
-            const float rows_ext = rowspan_max * fabsf(tau);
+            // Row extent in cells: |dB tau|, the frame's step.
+            const float rows_ext = fabsf(wcur.zf.sg);
             const bool wide = __any_sync(0xffffffffu, (hi - fk) > 4.0f || rows_ext > 1.99f);
             if (wcur.fits && !wide) {
                 float ov[4];
@@ -426,29 +417,30 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
                 const bool mid = __any_sync(0xffffffffu, rows_ext > 0.99f);
                 const float *patch = &sm.buf[b][0][k0 - wcur.kb];
                 if (nt == 2) {
-                    if (mid) sweep_tile<2, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
-                    else sweep_tile<2, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    if (mid) sweep_tile<2, true, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
+                    else sweep_tile<2, false, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
                 } else if (nt == 3) {
-                    if (mid) sweep_tile<3, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
-                    else sweep_tile<3, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    if (mid) sweep_tile<3, true, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
+                    else sweep_tile<3, false, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
                 } else {
-                    if (mid) sweep_tile<4, true, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
-                    else sweep_tile<4, false, TR>(patch, wcur.lb, ov, sm.bj2, A, tau, g, acc);
+                    if (mid) sweep_tile<4, true, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
+                    else sweep_tile<4, false, TR>(patch, wcur.lb, ov, wcur.zf, g, acc);
                 }
             } else {
                 // Cell-by-cell overlap from global memory; row values go through
                 // shared memory so the row loop stays rolled (small code).
                 const float *__restrict__ slab = src + (long long)s * st_s;
                 const int ka = max(k0, 0), kz = min((int)floorf(hi), nB - 1);
+                // Row boundaries in the slice's frame (local z, integer part ib).
+                const int ib = (int)wcur.zf.ibf;
                 for (int j = 0; j < kTR; ++j) {
-                    const float bja = (Sz - Bzr[min(r0 + j, nv)]) * inv_dz;
-                    const float bjb = (Sz - Bzr[min(r0 + j + 1, nv)]) * inv_dz;
-                    const float za = fmaf(bja, tau, A), zb = fmaf(bjb, tau, A);
+                    const float za = fmaf((float)j, wcur.zf.sg, wcur.zf.f);
+                    const float zb = fmaf((float)(j + 1), wcur.zf.sg, wcur.zf.f);
                     const float zlo = fminf(za, zb), zhi = fmaxf(za, zb);
-                    const int l0 = max((int)floorf(zlo), 0), l1 = min((int)floorf(zhi), nZ - 1);
+                    const int l0 = max((int)floorf(zlo) + ib, 0), l1 = min((int)floorf(zhi) + ib, nZ - 1);
                     float v = 0.0f;
                     for (int l = l0; l <= l1; ++l) {
-                        const float wz = fminf((float)(l + 1), zhi) - fmaxf((float)l, zlo);
+                        const float wz = fminf((float)(l - ib + 1), zhi) - fmaxf((float)(l - ib), zlo);
                         const float *__restrict__ row = slab + (long long)l * st_l;
                         float hx = 0.0f;
                         for (int k = ka; k <= kz; ++k)
@@ -487,7 +479,7 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         const int r = r0 + j;
         if (r < nv) {
             const float t2 = (Sz - Pzr[r]) * invD;
-            const float K = base * sqrtf(1.0f + t2 * t2) / fabsf(Bj[j + 1] - Bj[j]);
+            const float K = base * sqrtf(1.0f + t2 * t2) / rowspan_max;
             proj[((long long)vi * nv + r) * nu + c] = (j < kTR / 2 ? acc[j].x : acc[j - kTR / 2].y) * K;
         }
     }

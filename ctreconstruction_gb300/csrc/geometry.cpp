@@ -171,10 +171,16 @@ extern "C" int ctgb_table_build(const ctgb_params *p, void *host_table, size_t b
         }
         // numba: z = S_z - v with v = (r-(nv-1)/2)*dv (-+ dv/2 for boundaries);
         // pycuda: z = S_z + v with v = (r-(nv-1)/2)*(-dv) (+ dv/2) + offset.
-        for (int r = 0; r <= nv; ++r) {
-            double z = pyc ? S[2] + ((r - (nv - 1) / 2.0) * -p->dv + p->dv / 2.0 + voff)
-                           : S[2] - ((r - (nv - 1) / 2.0) * p->dv - p->dv / 2.0);
-            V[vo.bz + r] = (float)z;
+        auto zb = [&](int r) {
+            return pyc ? S[2] + ((r - (nv - 1) / 2.0) * -p->dv + p->dv / 2.0 + voff)
+                       : S[2] - ((r - (nv - 1) / 2.0) * p->dv - p->dv / 2.0);
+        };
+        for (int r = 0; r <= nv; ++r) V[vo.bz + r] = (float)zb(r);
+        // Row-boundary model in the forward's z units (dz is the signed spacing).
+        {
+            const double b0 = (S[2] - zb(0)) / dz, bn = (S[2] - zb(nv)) / dz;
+            V[VF_B0] = (float)b0;
+            V[VF_DB] = (float)((bn - b0) / nv);
         }
         for (int r = 0; r < nv; ++r) {
             double z = pyc ? S[2] + ((r - (nv - 1) / 2.0) * -p->dv + voff) : S[2] - (r - (nv - 1) / 2.0) * p->dv;
