@@ -370,6 +370,95 @@ def _timed(fn, steps, warmup):
     return a.elapsed_time(b) / steps
 
 
+def _timed_stages(stages, steps, warmup):
+    """Run the (name, fn) stages in order `steps` times after `warmup` untimed
+    rounds; CUDA events on the current stream around every stage.  Returns
+    (ms per round, {name: ms per round})."""
+    import torch
+    for _ in range(warmup):
+        for _, fn in stages:
+            fn()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    marks = []
+    first = torch.cuda.Event(enable_timing=True)
+    first.record(stream)
+    for _ in range(steps):
+        row = []
+        for _, fn in stages:
+            fn()
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(stream)
+            row.append(e)
+        marks.append(row)
+    torch.cuda.synchronize()
+    per = {name: 0.0 for name, _ in stages}
+    prev = first
+    for row in marks:
+        for (name, _), e in zip(stages, row):
+            per[name] += prev.elapsed_time(e)
+            prev = e
+    total = first.elapsed_time(marks[-1][-1]) / steps
+    return total, {k: v / steps for k, v in per.items()}
+
+
+def _lib_call(name, *args):
+    """A C-ABI call whose tensor arguments become device pointers and whose
+    float/int arguments pass through; the element count of the first tensor
+    and the current stream are appended (the element-wise iterative updates'
+    signature)."""
+    import ctypes
+    import torch
+    from ctreconstruction_gb300 import _lib
+    conv = [ctypes.c_void_p(a.data_ptr()) if isinstance(a, torch.Tensor) else a for a in args]
+    first = next(a for a in args if isinstance(a, torch.Tensor))
+    _lib.call(name, *conv, first.numel(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
+def hbm_roofline(kernel, ms_per_launch, alg_bytes, what):
+    """roofline object for an HBM-bound kernel: algorithmic bytes per launch
+    (`what` says how they are counted) over its CUDA-event time per launch,
+    against the measured copy bandwidth."""
+    peak, kind = measured_peaks()
+    achieved = alg_bytes / (ms_per_launch / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": kind, "traffic": profiled_traffic(kernel),
+            "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": ms_per_launch, "bytes_model": what}
+
+
+def ref_voxel_view_rate(params, views, vol=None, nthreads=None):
+    """CPU: the reference's CUDA-C kernels compiled for the host
+    (distance_project_on_*3 forward, flat_distance_backproj_arb2 backward)
+    on `views` of one scan, all host threads.  Returns (seconds per
+    voxel-view for forward + backward, forward s, backward s, kind, what)."""
+    from oracle import ref_runner
+    nthreads = nthreads or os.cpu_count()
+    n = params['NumberOfImage']
+    nvox = int(n[0]) * int(n[1]) * int(n[2])
+    if vol is None:
+        vol = np.random.default_rng(0).random((n[2], n[1], n[0]), dtype=np.float32)
+    if not ref_runner.available():
+        from oracle.oracle import OracleGeometry
+        g = OracleGeometry(params)
+        t0 = time.perf_counter()
+        pv = [g.forward(vol, v, 1, nthreads).astype(np.float32) for v in views]
+        t1 = time.perf_counter()
+        for v, q in zip(views, pv):
+            g.backward_fdk(q, v, 1, nthreads)
+        t2 = time.perf_counter()
+        return (t2 - t0) / (2.0 * nvox * len(views)), t1 - t0, t2 - t1, "port", "FP64 C oracle port, OpenMP"
+    r = ref_runner.RefScan(dict(params, DetectorOffset=[0.0, 0.0]))
+    t0 = time.perf_counter()
+    pv = [r.forward_view(vol, v, nthreads) for v in views]
+    t1 = time.perf_counter()
+    out = None
+    for v, q in zip(views, pv):
+        out = r.backward_view(q, v, r.angles[1] - r.angles[0], out=out, nthreads=nthreads)
+    t2 = time.perf_counter()
+    return ((t2 - t0) / (2.0 * nvox * len(views)), t1 - t0, t2 - t1, "reference",
+            "reference CUDA-C kernels (distance_project_on_*3, flat_distance_backproj_arb2) as host C++, OpenMP")
+
+
 def run_fdk128(args):
     """FDK 128^3 (1 mm), 360 views, 256x192 detector (1.5 mm), SAD 1000, SDD
     1500; modified Shepp-Logan, DD-forward projections with Poisson noise at
@@ -388,20 +477,55 @@ def run_fdk128(args):
     proj = -torch.log(torch.clamp(counts, min=1.0) / 1e5)
     q = torch.empty_like(proj)
     out = torch.empty(P.volume_shape, device=P.device)
-
-    def step():
-        q.copy_(proj)
-        P.filter(q)
-        P.backproject_fdk(q, out=out)
-
-    ms = _timed(step, args.steps, args.warmup)
+    integ = P.integrate(proj)
+    # backward() = integrate_rows_kernel + bp_fdk_integ_kernel (the launches
+    # backproject_fdk makes), issued as separate stages so each is timed.
+    stages = [("copy", lambda: q.copy_(proj)), ("filter", lambda: P.filter(q)),
+              ("integrate", lambda: P.integrate(q, out=integ)),
+              ("backproject", lambda: P.backproject_fdk_integrated(integ, out=out))]
+    ms, per = _timed_stages(stages, args.steps, args.warmup)
+    ms -= per["copy"]                      # restoring the input is not part of the step
     vv = 128 ** 3 * 360
     inner = ph.abs() > 0
     rmse = float(torch.sqrt(torch.mean((out - ph)[inner] ** 2)))
+    dom = max(("filter", "backproject"), key=lambda k: per[k])
+    if dom == "backproject":
+        roof = hbm_roofline("bp_fdk_integ_kernel", per["backproject"], 4.0 * vv, "4 B per voxel-view")
+    else:
+        roof = hbm_roofline("fdk_filter_kernel", per["filter"], 8.0 * 360 * 256 * 192, "8 B per detector pixel")
+    roof["per_stage_ms"] = per
+    cpu = None
+    if not args.no_cpu:
+        # The reference's CPU path for this configuration: Filtering() in NumPy
+        # (the FP64 restatement, oracle.fdk_filter) and the reference's
+        # backprojection kernel for every view, all host threads.
+        from oracle import ref_runner
+        from oracle.oracle import OracleGeometry
+        host = proj.cpu().numpy()
+        nthreads = os.cpu_count()
+        t0 = time.perf_counter()
+        filt = OracleGeometry(p).filtering(host).astype(np.float32)
+        t1 = time.perf_counter()
+        if ref_runner.available():
+            r = ref_runner.RefScan(dict(p, DetectorOffset=[0.0, 0.0], ReconCenter=[0, 0, 0]))
+            acc = None
+            for v in range(360):
+                acc = r.backward_view(filt[v], v, r.angles[1] - r.angles[0], out=acc, nthreads=nthreads)
+            kind, what = "reference", "flat_distance_backproj_arb2 as host C++ (OpenMP) + NumPy Filtering"
+        else:
+            OracleGeometry(p).backward_fdk(filt, 0, 360, nthreads)
+            kind, what = "port", "FP64 C oracle port (OpenMP) + NumPy Filtering"
+        t2 = time.perf_counter()
+        cpu = {"value": vv / (t2 - t0) / 1e9, "unit": UNIT, "cores": nthreads, "kind": kind,
+               "sample": "the whole workload (360 views, 128^3): " + what, "filter_s": t1 - t0,
+               "backproject_s": t2 - t1}
     return {"metric": "FDK reconstruction throughput", "value": vv / (ms / 1e3) / 1e9, "unit": UNIT,
             "ms_per_step": ms, "higher_is_better": True, "dtype": "f32", "data": "synthetic (Shepp-Logan, Poisson)",
-            "config": {"workload": "fdk_128cube_360views_det256x192", "step": "Filtering() + backward()"},
-            "rmse_vs_phantom_inside": rmse}
+            "config": {"workload": "fdk_128cube_360views_det256x192", "step": "Filtering() + backward()",
+                       "l2": "volume 8 MiB and projections 70 MiB fit L2: after the first step the inputs are "
+                             "L2-resident (upper bound on HBM-bound throughput)"},
+            "gpu_launches": (1 + 2) * args.steps, "rmse_vs_phantom_inside": rmse, "roofline": roof,
+            "cpu_baseline": cpu}
 
 
 def run_fan_batch(args):
@@ -443,12 +567,10 @@ def run_fan_batch(args):
         batch.filter(work)
         batch.backproject(work, images)            # autotunes the tile once (untimed)
 
-        def step():
-            work.copy_(flat)
-            batch.filter(work)
-            batch.backproject(work, images)
-
-        ms = _timed(step, args.steps, args.warmup)
+        stages = [("copy", lambda: work.copy_(flat)), ("filter", lambda: batch.filter(work)),
+                  ("backproject", lambda: batch.backproject(work, images))]
+        ms, per = _timed_stages(stages, args.steps, args.warmup)
+        ms -= per["copy"]
         imgs = batch.unpack(images)
         errs = []
         for i, t in truth:
@@ -457,14 +579,37 @@ def run_fan_batch(args):
         rmse["arc" if arc else "line"] = errs
         pv = sum(n * n for n in sizes) * nviews
         out["arc" if arc else "line"] = {"ms_per_batch": ms, "Gpixel_views_per_s": pv / (ms / 1e3) / 1e9,
-                                         "tile": list(batch.tile), "fitted_rel_err_slices_0_86_171": rmse["arc" if arc else "line"]}
+                                         "per_stage_ms": per, "tile": list(batch.tile),
+                                         "fitted_rel_err_slices_0_86_171": rmse["arc" if arc else "line"]}
+        if not arc:
+            line_sino, line_slice = sinos[0].cpu().numpy(), slices[0]
     total_ms = out["line"]["ms_per_batch"] + out["arc"]["ms_per_batch"]
     pv = sum(n * n for n in sizes) * nviews
+    # Dominant kernel: the persistent backprojection (one launch per batch).
+    bp_ms = max(out["line"]["per_stage_ms"]["backproject"], out["arc"]["per_stage_ms"]["backproject"])
+    roof = hbm_roofline("fan_bp_kernel", bp_ms, 4.0 * pv, "4 B per pixel-view")
+    cpu = None
+    if not args.no_cpu:
+        # FanBeam.py's own reconstruction restated in FP64 NumPy
+        # (oracle/standalone: Filter + per-view interpolated backprojection) on
+        # one 256^2 slice over all 720 views (NumPy's own threads).
+        from oracle import standalone as osa
+        n = 256
+        x = (np.arange(n) - (n - 1) / 2.0) * 0.8
+        ang = np.arange(nviews) * (2 * np.pi / nviews)
+        t0 = time.perf_counter()
+        Q, gam = osa.fan_filter(line_sino, sad, sdd, pitch, False, 'hann', 1.0)
+        osa.fan_backproject(Q, gam, x, x, sad, sdd, ang, False)
+        t1 = time.perf_counter()
+        cpu = {"value": n * n * nviews / (t1 - t0) / 1e9, "unit": "Gpixel*views/s", "cores": 1, "kind": "port",
+               "sample": "one 256^2 slice, 720 views, line detector: FanBeam.py's filter and backprojection "
+                         "restated in FP64 NumPy (oracle/standalone.py)", "seconds": t1 - t0}
     return {"metric": "batched fan-beam FBP throughput", "value": 2 * pv / (total_ms / 1e3) / 1e9,
             "unit": "Gpixel*views/s", "ms_per_step": total_ms, "higher_is_better": True, "dtype": "f32",
             "data": "synthetic (20 random ellipses per slice, exact line integrals)",
-            "config": {"workload": "fan_batch_256slices_720views_984ch", "detectors": ["line", "arc"]},
-            "detail": out}
+            "config": {"workload": "fan_batch_256slices_720views_984ch", "detectors": ["line", "arc"],
+                       "l2": "sinograms 725 MB and images 172 MB per detector exceed L2"},
+            "gpu_launches": 4 * args.steps, "roofline": roof, "cpu_baseline": cpu, "detail": out}
 
 
 def run_iter(args):
@@ -513,6 +658,33 @@ def run_iter(args):
     em_batch = iterative.SolverBatch([iterative.MLEM(Projector(p, device=dev), q.clamp(min=0)) for p, q, _ in scans])
     t_em = time_batch(em_batch, max(1, args.steps))
     del em_batch
+    # Dominant kernel: one OS-SART sub-iteration of the largest scan (384^3,
+    # 9 views) issued eagerly, each launch group timed alone (inside the graph
+    # the launches of 16 scans overlap and cannot be timed one by one).
+    p_big, q_big, _ = scans[-1]
+    solver = iterative.OSSART(Projector(p_big, device=dev), q_big, nsubsets=10, lam=0.8)
+    Ps, ps0, a1, b1 = solver.subsets[0]
+    S, x = solver.S, solver.x
+    stages = [("forward", lambda: Ps.forward(x, out=S.proj)),
+              ("residual", lambda: _lib_call("ctgb_pocs_residual", ps0, S.proj, a1, solver.eps, S.res)),
+              ("backproject_matched", lambda: iterative._backproject(Ps, S.res, S.bp, True)),
+              ("update", lambda: _lib_call("ctgb_pocs_update", x, S.bp, b1, solver.lam, solver.eps, x))]
+    _, per = _timed_stages(stages, 3, 2)
+    nb = sides[-1]
+    vv_sub = float(nb) ** 3 * 9
+    dom = max(("forward", "backproject_matched"), key=lambda k: per[k])
+    roof = hbm_roofline({"forward": "dd_forward_tma_kernel",
+                         "backproject_matched": "bp_matched_integ_kernel"}[dom], per[dom], 4.0 * vv_sub,
+                        "4 B per voxel-view (one 9-view subset of the 384^3 scan; the backprojection's time "
+                        "includes its integration pass)")
+    roof["per_stage_ms_384cube_subset"] = per
+    del solver
+    cpu = None
+    if not args.no_cpu:
+        spv, tf, tb, kind, what = ref_voxel_view_rate(p_big, [0])
+        cpu = {"value": 1.0 / spv / 1e9, "unit": UNIT + " (forward + backprojection)", "cores": os.cpu_count(),
+               "kind": kind, "sample": "one view forward + one view backward of the 384^3 scan: " + what,
+               "forward_s": tf, "backward_s": tb}
     # voxel-views per batch iteration: one forward + one backprojection per view
     return {"metric": "batched OS-SART iteration throughput", "value": 2 * vv / (t_os / 1e3) / 1e9,
             "unit": UNIT + " (forward + backprojection)", "ms_per_step": t_os, "higher_is_better": True,
@@ -522,6 +694,7 @@ def run_iter(args):
             "os_sart_ms_per_iteration": t_os, "mlem_ms_per_iteration": t_em,
             "mlem_value": 2 * vv / (t_em / 1e3) / 1e9,
             "os_sart_20_iterations_s": 20 * t_os / 1e3, "mlem_50_iterations_s": 50 * t_em / 1e3,
+            "gpu_launches": None, "roofline": roof, "cpu_baseline": cpu,
             "os_sart_rmse_after_%d_iterations" % (2 + max(1, args.warmup) + max(1, args.steps)): os_rmse[:4]}
 
 
@@ -545,10 +718,55 @@ def run_asd256(args):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / 3
+    roof, cpu = _asd_roofline_cpu(P, x, args)
     return {"metric": "ASD-POCS outer-iteration time", "value": ms, "unit": "ms", "higher_is_better": False,
             "dtype": "f32", "data": "synthetic (random ellipsoids)",
             "config": {"workload": "asd_pocs_256cube_60views_det512x384", "na": 5, "ng": 20, "alpha": 0.002},
-            "rmse_per_iteration": rmse}
+            "rmse_per_iteration": rmse, "gpu_launches": None, "roofline": roof, "cpu_baseline": cpu}
+
+
+def _asd_roofline_cpu(P, x, args, niter_label="outer iteration"):
+    """Roofline of the dominant kernel of one ASD-POCS outer iteration at
+    256^3 / 60 views (its five data sub-steps' forward and FDK-weighted
+    backprojection, and the 20-step TV descent, each timed alone), and the
+    reference's CPU cost of one outer iteration extrapolated from one view
+    forward + one view backward and one NumPy TV gradient."""
+    import torch
+    from ctreconstruction_gb300 import iterative
+    proj = torch.empty(P.proj_shape(), device=P.device)
+    vol = torch.empty(P.volume_shape, device=P.device)
+    xt = x.clone()
+    stages = [("forward", lambda: P.forward(x, out=proj)), ("backproject", lambda: P.backproject_fdk(proj, out=vol)),
+              ("tv20", lambda: iterative.tv_descent(xt, 1e-6, 20))]
+    _, per = _timed_stages(stages, 3, 2)
+    n = P.volume_shape[0]
+    vv = float(n) ** 3 * P.params.NumberOfViews
+    nfwd = P.forward_launches()
+    cand = {"forward": (per["forward"] / nfwd, 4.0 * vv / nfwd, "dd_forward_tma_kernel", "4 B per voxel-view"),
+            "backproject": (per["backproject"], 4.0 * vv, "bp_fdk_integ_kernel",
+                            "4 B per voxel-view (time includes the integration pass)"),
+            "tv20": (per["tv20"] / 20, 12.0 * n ** 3, "tv_norm_kernel + tv_step_kernel",
+                     "12 B per voxel per TV step (read for the norm; read + write for the step)")}
+    # dominant: the largest share of one outer iteration (5 forward + 5 backprojections + 1 TV descent)
+    share = {"forward": 5 * per["forward"], "backproject": 5 * per["backproject"], "tv20": per["tv20"]}
+    dom = max(share, key=share.get)
+    ms_l, by, kname, what = cand[dom]
+    roof = hbm_roofline(kname, ms_l, by, what)
+    roof["per_stage_ms"] = per
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as ora
+        spv, tf, tb, kind, what = ref_voxel_view_rate(P.params.as_dict(), [0])
+        xh = x.cpu().numpy()
+        t0 = time.perf_counter()
+        ora.tv_grad(xh)
+        t_tv = time.perf_counter() - t0
+        ms_cpu = (5 * 2 * vv * spv + 20 * t_tv) * 1e3
+        cpu = {"value": ms_cpu, "unit": "ms per " + niter_label, "cores": os.cpu_count(), "kind": kind,
+               "sample": "extrapolated from one view forward + one view backward at 256^3 (" + what + ") and "
+                         "one NumPy TV gradient (ASD_POCS.py tv_grad restated): 5 x (60-view forward + "
+                         "60-view backward) + 20 TV steps", "tv_grad_s": t_tv, "forward_s": tf, "backward_s": tb}
+    return roof, cpu
 
 
 def run_asd256_learned(args):
@@ -598,12 +816,23 @@ def run_asd256_learned(args):
     t_plain = []
     _, rmse_plain, _ = iterative.asd_pocs(P, proj0, niter=niter, norms=norms, phantom=ph, times=t_plain, x0=zero,
                                           **asd)
+    # Warm the learned step at the full volume size (the network was trained
+    # on crops: its first 256^3 call builds tensor maps and sets kernel
+    # attributes), as the plain step was warmed above.
+    warm = learned.LearnedProx(net, P, proj0, tol=0.01, judge_every=1)
+    warm(zero.clone(), lambda: iterative.tv_descent(zero.clone(), 1e-6, asd["ng"]))
+    torch.cuda.synchronize()
     prox = learned.LearnedProx(net, P, proj0, tol=0.01, judge_every=1)
     t_learn = []
     _, rmse_learn, _ = iterative.asd_pocs(P, proj0, niter=niter, norms=norms, phantom=ph, prox=prox,
                                           times=t_learn, x0=zero, **asd)
     target = 1.01 * rmse_plain[-1]
     reach = next((i for i, r in enumerate(rmse_learn) if r <= target), None)
+    # FDK (Filtering() + backward()) of the same data, for scale: the RMSE
+    # the iterative runs are measured against.
+    fq = proj0.clone()
+    P.filter(fq)
+    rmse_fbp = float(torch.sqrt(torch.mean((P.backproject_fdk(fq) - ph) ** 2)))
     # U-Net forward alone at 256^3 and the 20-step TV descent it replaces
     x = ph.clone()
     net.forward(x, net.scale)
@@ -621,6 +850,16 @@ def run_asd256_learned(args):
     torch.cuda.synchronize()
     tv_ms = a.elapsed_time(b)
     flops = learned.FLOPS_PER_VOXEL * 256 ** 3
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            bpeak, bkind = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        bpeak, bkind = 1900.0, "fallback"
+    tf = flops / (unet_ms / 1e3) / 1e12
+    roof = {"bound": "tensor", "kernel": "conv3d_tc_dx_kernel (U-Net forward, all layers)", "achieved": tf,
+            "peak": bpeak, "unit": "TFLOP/s", "frac": tf / bpeak, "peak_source": bkind, "flops_per_pass": flops,
+            "ms_per_pass": unet_ms}
+    _, cpu = _asd_roofline_cpu(P, ph, args, "plain outer iteration")
     return {"metric": "learned ASD-POCS wall time to the plain RMSE (x1.01), relative to plain",
             "value": (t_learn[reach] / t_plain[-1]) if reach is not None else None, "unit": "ratio",
             "higher_is_better": False, "dtype": "bf16 U-Net / f32 projectors",
@@ -628,12 +867,14 @@ def run_asd256_learned(args):
             "config": {"workload": "asd_pocs_learned_256cube_60views_det512x384", "alpha": 0.002, "ng": 20,
                        "na": 5, "iterations": niter, "pairs": n_pairs, "train_steps": args.train_steps,
                        "pair_ahead": args.ahead},
-            "rmse_plain": rmse_plain, "rmse_learned": rmse_learn, "plain_s": t_plain[-1],
+            "rmse_plain": rmse_plain, "rmse_learned": rmse_learn, "rmse_fbp": rmse_fbp, "plain_s": t_plain[-1],
+            "learned_s_cumulative": t_learn,
             "learned_s_per_iteration": t_learn[-1] / niter, "plain_s_per_iteration": t_plain[-1] / niter,
             "learned_reaches_target_at_iteration": reach, "accepted": prox.accepted, "rejected": prox.rejected,
             "train_loss_first_last": [float(np.mean(losses[:10])), float(np.mean(losses[-10:]))],
             "pairs_s": t_pairs, "train_s": t_train, "unet_forward_ms_256cube": unet_ms,
-            "unet_tflops": flops / (unet_ms / 1e3) / 1e12, "tv20_ms_256cube": tv_ms}
+            "unet_tflops": flops / (unet_ms / 1e3) / 1e12, "tv20_ms_256cube": tv_ms, "roofline": roof,
+            "cpu_baseline": cpu}
 
 
 def run_rows(args):
@@ -666,11 +907,10 @@ def run_rows(args):
         proj = torch.empty(P.proj_shape(), device=dev)
         vol = torch.empty_like(ph)
 
-        def pair(P=P, proj=proj, vol=vol):
-            P.forward(ph, out=proj)
-            P.backproject_fdk(proj, out=vol)
-
-        detail[name] = rate(_timed(pair, args.steps, args.warmup))
+        stages = [("forward", lambda P=P, proj=proj: P.forward(ph, out=proj)),
+                  ("backproject", lambda P=P, proj=proj, vol=vol: P.backproject_fdk(proj, out=vol))]
+        ms, per = _timed_stages(stages, args.steps, args.warmup)
+        detail[name] = dict(rate(ms), per_stage_ms=per)
     P = Projector(dict(base, Method='Ray'), device=dev)
     proj = torch.empty(P.proj_shape(), device=dev)
     vol = torch.empty_like(ph)
@@ -696,11 +936,36 @@ def run_rows(args):
                   _stream())
 
     detail["conebeam_fdk_backprojection"] = rate(_timed(cone_bp, args.steps, args.warmup))
+    per = detail["dd_pair_curved"]["per_stage_ms"]
+    dom = max(per, key=per.get)
+    nfwd = Projector(dict(base, DetectorShape='Curved'), device=dev).forward_launches()
+    roof = hbm_roofline({"forward": "dd_forward_tma_kernel", "backproject": "bp_fdk_integ_kernel"}[dom],
+                        per[dom] / (nfwd if dom == "forward" else 1), 4.0 * vv / (nfwd if dom == "forward" else 1),
+                        "4 B per voxel-view, curved detector (backprojection time includes its integration pass)")
+    cpu = None
+    if not args.no_cpu:
+        # Curved detectors run only in the reference's numba flavour (its
+        # pycuda curved backprojector is called with 8 of 17 arguments), so
+        # the CPU baseline is the FP64 C oracle port of that flavour.
+        from oracle.oracle import OracleGeometry
+        g = OracleGeometry(dict(base, DetectorShape='Curved'))
+        vol_h = ph.cpu().numpy()
+        nthreads = os.cpu_count()
+        t0 = time.perf_counter()
+        pv = g.forward(vol_h, 7, 1, nthreads).astype(np.float32)
+        t1 = time.perf_counter()
+        g.backward_fdk(pv, 7, 1, nthreads)
+        t2 = time.perf_counter()
+        cpu = {"value": 2.0 * n ** 3 / (t2 - t0) / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": "one view forward + one view FDK-weighted backprojection at %d^3, curved detector: FP64 C "
+                         "oracle port (OpenMP)" % n, "forward_s": t1 - t0, "backward_s": t2 - t1}
     return {"metric": "hot-path rows throughput (curved DD pair; detail: helical, flat, Siddon, voxel-driven FDK)",
             "value": detail["dd_pair_curved"]["Gvoxel_views_per_s"], "unit": UNIT,
             "ms_per_step": detail["dd_pair_curved"]["ms"], "higher_is_better": True, "dtype": "f32",
             "data": "synthetic (30 seeded random ellipsoids; uniform random projections for the voxel-driven BP)",
-            "config": {"workload": "rows_%dcube_%dviews_det%dx%d" % (n, nviews, nu, nv)}, "detail": detail}
+            "config": {"workload": "rows_%dcube_%dviews_det%dx%d" % (n, nviews, nu, nv),
+                       "l2": "volume 64 MiB (fits L2), projections 283 MB"},
+            "gpu_launches": None, "roofline": roof, "cpu_baseline": cpu, "detail": detail}
 
 
 def run_unet(args):
@@ -721,11 +986,24 @@ def run_unet(args):
     except Exception:
         peak, kind = 1900.0, "fallback"
     tf = flops / (ms / 1e3) / 1e12
+    cpu = None
+    if not args.no_cpu:
+        # The FP64 NumPy restatement of the network (oracle/unet.py, bf16
+        # rounding emulated) on a 16 x 32 x 32 crop.
+        from oracle import unet as ounet
+        params = {k: v.detach().cpu().numpy() for k, v in net.params.items()}
+        xc = x[:16, :32, :32].cpu().numpy()[None]
+        t0 = time.perf_counter()
+        ounet.forward(params, xc, np.array([0.01]))
+        t1 = time.perf_counter()
+        cpu = {"value": learned.FLOPS_PER_VOXEL * xc.size / (t1 - t0) / 1e12, "unit": "TFLOP/s", "cores": 1,
+               "kind": "port", "sample": "U-Net forward on a 16x32x32 crop: FP64 NumPy restatement "
+                                         "(oracle/unet.py)", "seconds": t1 - t0}
     return {"metric": "3-D U-Net forward throughput", "value": tf, "unit": "TFLOP/s", "ms_per_step": ms,
             "higher_is_better": True, "dtype": "bf16 (fp32 accumulate)", "data": "synthetic (random ellipsoids)",
             "config": {"workload": "unet3d_forward_%dcube" % n, "levels": 3, "channels": [16, 32, 64]},
             "roofline": {"bound": "tensor", "achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
-                         "peak_source": kind, "flops_per_pass": flops}}
+                         "peak_source": kind, "flops_per_pass": flops}, "cpu_baseline": cpu}
 
 
 WORKLOADS = {"rows": run_rows, "unet": run_unet, "fdk128": run_fdk128, "fan_batch": run_fan_batch, "iter": run_iter, "asd256": run_asd256,
