@@ -309,22 +309,29 @@ def run_ours(args):
     host_vol = vol.cpu().numpy()
     pinned_vol = torch.from_numpy(host_vol).pin_memory()
     R = Reconstruction(params, device=dev)
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = max(1, min(args.steps, 10))
     R.image = pinned_vol
     R.forward()
     R.backward()
     barrier()
+    fwd_ms, bwd_ms = [], []
     with ClockSampler(local, "e2e") as clk_e2e:
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            ta = time.perf_counter()
             R.image = pinned_vol
             R.forward()
+            tb = time.perf_counter()
             R.backward()
+            tc = time.perf_counter()
+            fwd_ms.append((tb - ta) * 1e3)
+            bwd_ms.append((tc - tb) * 1e3)
         barrier()
         e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e = {"value": ws * vv / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+    e2e = {"value": ws * vv / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3, "steps": e2e_steps,
            "h2d_bytes_per_step": int(4 * (n ** 3 + nviews * P.params.nu * P.params.nv)),
            "d2h_bytes_per_step": int(4 * (n ** 3 + nviews * P.params.nu * P.params.nv)),
+           "forward_ms": [round(v, 2) for v in fwd_ms], "backward_ms": [round(v, 2) for v in bwd_ms],
            "clocks": clk_e2e.summary()}
 
     cpu = None

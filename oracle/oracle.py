@@ -247,6 +247,41 @@ def mlem(g, proj0, niter, eps=1e-5, x0=None):
     return x
 
 
+def os_sart(params, proj0, nsubsets, niter, lam=0.8, eps=1e-5, x0=None, flavour="numba"):
+    """Ordered-subsets SART as ctreconstruction_gb300.iterative.OSSART states
+    it (no reference counterpart; its update is ASD_POCS.py:171-179's POCS
+    step on one subset at a time), in float32 NumPy over the FP64 oracle
+    projectors with the matched (transposed) backprojection.  Subset s holds
+    views s, s + nsubsets, ...: the scan with StartAngle + s * dtheta and
+    NumberOfViews / nsubsets views.  Per subset:
+        r = (p0_s - A_s x) / (A_s 1 + eps), 0 where A_s 1 == 0
+        x = max(0, x + lam * B_s r / (B_s 1 + eps)), B_s r taken as 0 where B_s 1 == 0."""
+    f32 = np.float32
+    nv = int(params['NumberOfViews'])
+    span = float(params['EndAngle']) - float(params['StartAngle'])
+    dth = span / nv
+    subsets = []
+    for s in range(nsubsets):
+        d = dict(params)
+        d['StartAngle'] = float(params['StartAngle']) + s * dth
+        d['EndAngle'] = d['StartAngle'] + span
+        d['NumberOfViews'] = nv // nsubsets
+        g = OracleGeometry(d, flavour)
+        a1 = g.forward(np.ones((g.nz, g.ny, g.nx), np.float32)).astype(f32)
+        b1 = g.backward_matched(np.ones((g.nviews, g.nv, g.nu), np.float32)).astype(f32)
+        subsets.append((g, np.ascontiguousarray(proj0[s::nsubsets], dtype=f32), a1, b1))
+    g0 = subsets[0][0]
+    x = np.zeros((g0.nz, g0.ny, g0.nx), f32) if x0 is None else x0.astype(f32).copy()
+    for _ in range(niter):
+        for g, ps0, a1, b1 in subsets:
+            p = g.forward(x).astype(f32)
+            r = np.where(a1 == 0, f32(0), (ps0 - p) / (a1 + f32(eps))).astype(f32)
+            b = g.backward_matched(r).astype(f32)
+            b = np.where(b1 == 0, f32(0), b)
+            x = np.maximum(x + f32(lam) * b / (b1 + f32(eps)), f32(0)).astype(f32)
+    return x
+
+
 def tv_grad(image, eps=1e-7):
     """ASD_POCS.py:55-77 (np.lib.pad replaced by np.pad)."""
     f32 = np.float32

@@ -15,7 +15,7 @@ committed, so the tests never need the reference at run time.
 
 Inputs are seeded, so rerunning reproduces the files.
 
-    python tests/golden/make_golden.py /path/to/reference
+    python tests/golden/make_golden.py /path/to/reference [--only-fanbeam]
     CTGB_REFERENCE_ROOT=/path/to/reference python tests/golden/make_golden.py
 """
 import copy
@@ -161,6 +161,70 @@ def conebeam_golden(ref_root, lib_path):
     print("conebeam_ref: recon range", float(dest.min()), float(dest.max()))
 
 
+FAN_CASES = [
+    # name, params, ReconVolume (x*y), slices (DetectorHeight), seed
+    ("fanbeam_square", {'SourceToAxis': 57.0, 'SourceToDetector': 104.0, 'DetectorPixelWidth': 0.9,
+                        'DetectorWidth': 61, 'NumberOfViews': 48, 'AngleCoverage': 360.0}, (24, 24), 2, 400),
+    ("fanbeam_short", {'SourceToAxis': 80.0, 'SourceToDetector': 150.0, 'DetectorPixelWidth': 1.1,
+                       'DetectorWidth': 45, 'NumberOfViews': 36, 'AngleCoverage': 240.0}, (32, 32), 1, 401),
+]
+# (Reconstruction() supports square images only: it adds a [ReconX, ReconY]
+# reshape of the [ReconY, ReconX] interpolation grid to a [ReconY, ReconX]
+# weight, FanBeam.py:133-134, which does not broadcast otherwise.)
+
+
+def fanbeam_golden(ref_root):
+    """python/FanBeam.py's Reconstruction(), unmodified, on synthetic
+    sinograms.  Two defects stop it from running as written, and both are
+    bridged from outside the module, the way _numba_stub supplies numba:
+    * it calls ceil and log2 without importing them (FanBeam.py:89): they are
+      supplied as module attributes (math.ceil, math.log2);
+    * it hands interp1d the whole zero-padded filtered row Q (FanBeam.py:
+      119-128: length ZeroPaddedLength) against the nx detector positions
+      gamma, which scipy rejects: the module's interp1d is wrapped to take the
+      first nx samples, the truncation the reference's cone-beam scripts
+      make (ConeBeamGPU.py:300, Q[k, :] = tmp[0:nx]) and the only reading
+      under which the call is defined.
+    LoadData() is bypassed (it reads .dat files and keeps only one of them,
+    FanBeam.py:160-167): the sinogram [NumberOfViews][DetectorWidth]
+    [DetectorHeight] is set on the object directly.  Reconstruction() fixes
+    the filter at Hann, cutoff 0.3.  Writes tests/golden/<name>.npz with the
+    parameters, sinogram and reconstruction [ReconX][ReconY][DetectorHeight]."""
+    import math
+    import tempfile
+    import _numba_stub
+    _numba_stub.install()                    # also registers a matplotlib stand-in
+    sys.path.insert(0, os.path.join(ref_root, "python"))
+    import FanBeam as FB
+    FB.ceil, FB.log2 = math.ceil, math.log2
+    scipy_interp1d = FB.interp1d
+
+    def interp1d_first_n(x, y, **kw):
+        return scipy_interp1d(x, np.asarray(y)[..., :len(x)], **kw)
+
+    FB.interp1d = interp1d_first_n
+    for name, p, (rx, ry), nslices, seed in FAN_CASES:
+        with tempfile.TemporaryDirectory() as tmp:
+            pf = os.path.join(tmp, "ReconstructionParamsFan.txt")
+            with open(pf, "w") as f:
+                for k in ('SourceToAxis', 'SourceToDetector', 'DetectorPixelWidth', 'DetectorWidth',
+                          'NumberOfViews', 'AngleCoverage'):
+                    f.write("%s: %r\n" % (k, p[k]))
+                f.write("DetectorHeight: %d\n" % nslices)
+                f.write("ReconVolume: %d*%d\n" % (rx, ry))
+                f.write("DataPath: %s/\nprecision: float32\n" % tmp)
+            R = FB.FanBeam(pf)
+            rng = np.random.default_rng(seed)
+            sino = rng.random((int(p['NumberOfViews']), int(p['DetectorWidth']), nslices)).astype(np.float32)
+            R.sino = sino.astype(np.float64)
+            R.Reconstruction(os.path.join(tmp, "recon.dat"))
+            recon = np.asarray(R.recon, dtype=np.float32)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), params=json.dumps(dict(p, DetectorHeight=nslices,
+                                                                                         ReconX=rx, ReconY=ry)),
+                            sino=sino, recon=recon)
+        print("%s: recon %s range %.4g .. %.4g" % (name, recon.shape, recon.min(), recon.max()))
+
+
 def main(ref_root):
     sys.path.insert(0, os.path.join(ref_root, "python"))
     import _numba_stub
@@ -205,7 +269,12 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CTGB_REFERENCE_ROOT")
+    pos = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = pos[0] if pos else os.environ.get("CTGB_REFERENCE_ROOT")
     if not root or not os.path.isdir(os.path.join(root, "python")):
         sys.exit("make_golden.py: give the reference checkout as the first argument or in CTGB_REFERENCE_ROOT")
-    main(root)
+    if "--only-fanbeam" in sys.argv:
+        fanbeam_golden(root)
+    else:
+        main(root)
+        fanbeam_golden(root)

@@ -68,13 +68,30 @@ def test_tv_step_matches_tv_grad(cuda):
     assert rel_err(got3.cpu().numpy(), want3) < 1e-5
 
 
-def test_asd_pocs_matches_oracle(setup, cuda):
+@pytest.mark.parametrize("ng", [0, 3])
+def test_asd_pocs_matches_oracle(setup, cuda, ng):
+    """ASD-POCS (2 outer iterations, 2 POCS sub-steps, ng TV steps) against
+    the same loop over the FP64 oracle, at the common bar."""
     g, P, ph, proj0 = setup
-    want, log_o = ora.asd_pocs(g, proj0.copy(), 2, na=2, ng=3)
-    x, _, log_g = iterative.asd_pocs(P, torch.from_numpy(proj0).to(cuda), niter=2, na=2, ng=3)
-    assert rel_err(x.cpu().numpy(), want) < 5 * RTOL
+    want, log_o = ora.asd_pocs(g, proj0.copy(), 2, na=2, ng=ng)
+    x, _, log_g = iterative.asd_pocs(P, torch.from_numpy(proj0).to(cuda), niter=2, na=2, ng=ng)
+    err = rel_err(x.cpu().numpy(), want)
+    print("ASD-POCS ng=%d rel err %.3e" % (ng, err))
+    assert err < RTOL
     for a, b in zip(log_g, log_o):
         assert a["alpha"] == b["alpha"] and abs(a["dp"] - b["dp"]) <= 1e-3 * b["dp"]
+
+
+@pytest.mark.parametrize("nsubsets,niter", [(4, 3), (3, 2), (12, 1)])
+def test_os_sart_matches_oracle(setup, cuda, nsubsets, niter):
+    """OS-SART with several subsets against the same loop over the FP64
+    oracle projectors (oracle.os_sart)."""
+    g, P, ph, proj0 = setup
+    want = ora.os_sart(GEOM, proj0.copy(), nsubsets, niter, lam=0.8)
+    x, _ = iterative.os_sart(P, torch.from_numpy(proj0).to(cuda), nsubsets=nsubsets, niter=niter, lam=0.8)
+    err = rel_err(x.cpu().numpy(), want)
+    print("OS-SART nsubsets=%d niter=%d rel err %.3e" % (nsubsets, niter, err))
+    assert err < RTOL
 
 
 def test_os_sart_reduces_error(setup, cuda):

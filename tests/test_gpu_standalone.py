@@ -166,6 +166,24 @@ def test_fan_autotuner_is_tile_independent(cuda):
     assert torch.allclose(got, ref, rtol=1e-6, atol=1e-6 * ref.abs().max().item())
 
 
+@pytest.mark.parametrize("name", ["fanbeam_square", "fanbeam_short"])
+def test_fanbeam_class_matches_reference_fanbeam(cuda, tmp_path, name):
+    """The FanBeam class (one persistent batched launch) against
+    python/FanBeam.py's own Reconstruction() on the same sinogram
+    (tests/golden/fanbeam_*.npz, made by tests/golden/make_golden.py)."""
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    p = json.loads(str(d["params"]))
+    sino, want = d["sino"], d["recon"]                     # [views][channels][slices], [X][Y][slices]
+    params = dict(p, AngleCoverage=p['AngleCoverage'] * math.pi / 180.0)
+    stack = [sino[i].T for i in range(sino.shape[0])]       # per view: [slices][channels]
+    fname = _write_case(tmp_path, params, stack, "%d*%d" % (p['ReconX'], p['ReconY']))
+    fb = FanBeam(fname, device=cuda)
+    fb.LoadData()
+    fb.Reconstruction(str(tmp_path / "fan.dat"))
+    assert fb.recon.shape == want.shape
+    assert rel_err(fb.recon, want) < RTOL
+
+
 def test_fanbeam_class_line(cuda, tmp_path):
     params = {'SourceToAxis': 57.0, 'SourceToDetector': 104.0, 'DetectorPixelWidth': 0.9, 'DetectorWidth': 61,
               'DetectorHeight': 3, 'NumberOfViews': 40, 'AngleCoverage': 2 * math.pi}

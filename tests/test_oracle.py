@@ -73,3 +73,25 @@ def test_oracle_view_ranges_compose():
     whole = g.backward_fdk(y)
     split = g.backward_fdk(y[:5], 0, 5) + g.backward_fdk(y[5:], 5, 3)
     assert np.allclose(whole, split, rtol=1e-12, atol=1e-12)
+
+
+def test_os_sart_oracle_one_subset_is_the_pocs_formula():
+    """oracle.os_sart with one subset and one pass from zero is one POCS step
+    with the matched pair; two subsets of 3 views cover the 6-view scan."""
+    from oracle import oracle as ora
+    from _util import cone_params
+    p = cone_params(n=(10, 9, 8), nviews=6, nu=20, nv=16)
+    g = ora.OracleGeometry(p)
+    rng = np.random.default_rng(2)
+    proj0 = rng.random((6, 16, 20)).astype(np.float32)
+    got = ora.os_sart(p, proj0, 1, 1, lam=0.8)
+    a1 = g.forward(np.ones((8, 9, 10), np.float32))
+    b1 = g.backward_matched(np.ones((6, 16, 20), np.float32))
+    r = np.where(a1 == 0, 0, proj0 / (a1 + 1e-5))
+    b = g.backward_matched(r.astype(np.float32))
+    want = np.maximum(0.8 * np.where(b1 == 0, 0, b) / (b1 + 1e-5), 0)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+    subs = [ora.OracleGeometry(dict(p, StartAngle=s * 2 * np.pi / 6, EndAngle=s * 2 * np.pi / 6 + 2 * np.pi,
+                                    NumberOfViews=3)) for s in range(2)]
+    ang = np.sort(np.concatenate([q.angles for q in subs]))
+    assert np.allclose(ang, g.angles)

@@ -1,7 +1,8 @@
 """CPU checks of the standalone reconstructors' oracle and host logic:
 the FP64 restatement against the reference's own Filter functions and its
-compiled interpolation kernels (tests/golden/conebeam_ref.npz), and the
-"key: value" parameter-file parser."""
+compiled interpolation kernels (tests/golden/conebeam_ref.npz), against
+python/FanBeam.py's own Reconstruction() (tests/golden/fanbeam_*.npz), and
+the "key: value" parameter-file parser."""
 import json
 import os
 
@@ -28,6 +29,36 @@ def test_fan_spectrum_matches_reference_filter(key):
     _, _, ft, co = key.split("_")
     got = sa.standalone_filter(2049, 0.37, ft, float(co))
     assert rel_err(got, REF[key]) < 1e-12
+
+
+FAN_GOLDENS = ["fanbeam_square", "fanbeam_short"]
+
+
+def fan_golden(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return json.loads(str(d["params"])), d["sino"], d["recon"]
+
+
+def fan_oracle_slice(p, sino_slice):
+    """FanBeam.Reconstruction (FanBeam.py:82-138) of one slice through the
+    FP64 restatement: image [ReconY][ReconX] on linspace(-fov/2, fov/2)."""
+    R, sdd, pw, nx = p['SourceToAxis'], p['SourceToDetector'], p['DetectorPixelWidth'], p['DetectorWidth']
+    fov = 2 * R * np.sin(np.arctan(nx * pw / 2 / sdd))
+    x = np.linspace(-fov / 2, fov / 2, p['ReconX'])
+    ns = p['NumberOfViews']
+    ang = np.linspace(0, p['AngleCoverage'] * np.pi / 180.0, ns + 1)[:-1]
+    Q, gam = sa.fan_filter(sino_slice, R, sdd, pw, False, 'hann', 0.3)
+    return sa.fan_backproject(Q, gam, x, x, R, sdd, ang, False)
+
+
+@pytest.mark.parametrize("name", FAN_GOLDENS)
+def test_fan_oracle_matches_reference_fanbeam(name):
+    """The FP64 fan-beam restatement reproduces python/FanBeam.py's own
+    Reconstruction() (run unmodified by tests/golden/make_golden.py)."""
+    p, sino, recon = fan_golden(name)
+    for j in range(sino.shape[2]):
+        got = fan_oracle_slice(p, sino[:, :, j].astype(np.float64))
+        assert rel_err(got, recon[:, :, j]) < 1e-6, j
 
 
 def test_cone_filtering_and_backprojection_match_reference():
