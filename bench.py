@@ -623,10 +623,14 @@ def run_iter(args):
     """Batched OS-SART (10 subsets, lambda 0.8) and MLEM over 16 cone-beam
     scans, volumes 128^3..384^3 (multiples of 16), 90 views, detector 2N x 2N
     at 1.5x the voxel pitch, random ellipsoids with Poisson noise at I0 =
-    5e4.  Each method's 16 scans advance together: one CUDA graph holds one
-    iteration of all of them (OS-SART: 10 subsets each), so an iteration is
-    one graph launch.  Reports ms per batch iteration and the implied time
-    of the configured runs (20 OS-SART iterations, 50 MLEM iterations)."""
+    5e4.  Each method's 16 scans advance together (ctreconstruction_gb300.batch):
+    per OS-SART subset, one persistent forward launch per dominant axis and
+    one persistent backprojection over all 16 scans, with the update lines
+    fused into their stores; one CUDA graph holds one iteration, so an
+    iteration is one graph launch.  Reports ms per batch iteration and the
+    implied time of the configured runs (20 OS-SART iterations, 50 MLEM
+    iterations), and for comparison the same scans as concurrent per-scan
+    branches of one graph with separate element-wise kernels."""
     import torch
     from ctreconstruction_gb300 import Projector, iterative, phantoms
     sides = [int(round(v / 16.0)) * 16 for v in np.linspace(128, 384, 16)]
@@ -657,14 +661,23 @@ def run_iter(args):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / iters
 
-    os_batch = iterative.SolverBatch([iterative.OSSART(Projector(p, device=dev), q, nsubsets=10, lam=0.8)
-                                      for p, q, _ in scans])
+    from ctreconstruction_gb300 import batch
+    os_batch = batch.batched_os_sart([(Projector(p, device=dev), q) for p, q, _ in scans], nsubsets=10, lam=0.8)
     t_os = time_batch(os_batch, max(1, args.steps))
+    os_launches = os_batch.launches_per_step()
     os_rmse = [float(torch.sqrt(torch.mean((s.x - ph) ** 2))) for s, (_, _, ph) in zip(os_batch.solvers, scans)]
+    os_ctas = (os_batch.fwd_ctas, os_batch.bp_ctas)
     del os_batch
-    em_batch = iterative.SolverBatch([iterative.MLEM(Projector(p, device=dev), q.clamp(min=0)) for p, q, _ in scans])
+    em_batch = batch.batched_mlem([(Projector(p, device=dev), q.clamp(min=0)) for p, q, _ in scans])
     t_em = time_batch(em_batch, max(1, args.steps))
+    em_launches = em_batch.launches_per_step()
     del em_batch
+    # For comparison: the same solvers as concurrent per-scan branches of one
+    # CUDA graph, with separate element-wise kernels.
+    br = iterative.SolverBatch([iterative.OSSART(Projector(p, device=dev), q, nsubsets=10, lam=0.8)
+                                for p, q, _ in scans])
+    t_os_branches = time_batch(br, max(1, args.steps))
+    del br
     # Dominant kernel: one OS-SART sub-iteration of the largest scan (384^3,
     # 9 views) issued eagerly, each launch group timed alone (inside the graph
     # the launches of 16 scans overlap and cannot be timed one by one).
@@ -697,7 +710,13 @@ def run_iter(args):
             "unit": UNIT + " (forward + backprojection)", "ms_per_step": t_os, "higher_is_better": True,
             "dtype": "f32", "data": "synthetic (random ellipsoids, Poisson I0=5e4)",
             "config": {"workload": "os_sart_mlem_16scans_128to384_90views", "sides": sides,
-                       "graph": "one CUDA graph launch per batch iteration"},
+                       "graph": "one CUDA graph launch per batch iteration",
+                       "launches": "per OS-SART subset: one batched transpose, one persistent forward launch per "
+                                   "dominant axis (POCS residual fused), one integration, one persistent matched "
+                                   "backprojection (POCS update fused), all 16 scans in each",
+                       "persistent_ctas_per_sm_fwd_bp": os_ctas},
+            "os_sart_launches_per_iteration": os_launches, "mlem_launches_per_iteration": em_launches,
+            "os_sart_ms_per_iteration_per_scan_graph_branches": t_os_branches,
             "os_sart_ms_per_iteration": t_os, "mlem_ms_per_iteration": t_em,
             "mlem_value": 2 * vv / (t_em / 1e3) / 1e9,
             "os_sart_20_iterations_s": 20 * t_os / 1e3, "mlem_50_iterations_s": 50 * t_em / 1e3,

@@ -45,6 +45,26 @@ class CtgbFanSlice(ctypes.Structure):
                 ("pad", ctypes.c_int32), ("sino_offset", ctypes.c_int64), ("image_offset", ctypes.c_int64)]
 
 
+class CtgbFwdJob(ctypes.Structure):
+    """Mirror of ``ctgb_fwd_job`` (include/ctgb.h): one scan of a batched forward launch."""
+    _fields_ = [("params", ctypes.POINTER(CtgbParams)), ("table", ctypes.c_void_p), ("vol", ctypes.c_void_p),
+                ("vol_xzy", ctypes.c_void_p), ("out", ctypes.c_void_p), ("view0", ctypes.c_int32),
+                ("nviews", ctypes.c_int32), ("epilogue", ctypes.c_int32), ("eps", ctypes.c_float),
+                ("p0", ctypes.c_void_p), ("a1", ctypes.c_void_p)]
+
+
+class CtgbBpJob(ctypes.Structure):
+    """Mirror of ``ctgb_bp_job`` (include/ctgb.h): one scan of a batched backprojection launch."""
+    _fields_ = [("params", ctypes.POINTER(CtgbParams)), ("table", ctypes.c_void_p), ("proj", ctypes.c_void_p),
+                ("vol", ctypes.c_void_p), ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t),
+                ("view0", ctypes.c_int32), ("nviews", ctypes.c_int32), ("scale", ctypes.c_float),
+                ("accumulate", ctypes.c_int32), ("epilogue", ctypes.c_int32), ("coef", ctypes.c_float),
+                ("eps", ctypes.c_float), ("x", ctypes.c_void_p), ("n1", ctypes.c_void_p)]
+
+
+FWD_STORE, FWD_SART_RESIDUAL, FWD_POCS_RESIDUAL, FWD_EM_RATIO = 0, 1, 2, 3
+BP_STORE, BP_SART_UPDATE, BP_EM_UPDATE, BP_POCS_UPDATE = 0, 1, 2, 3
+
 # (name, argtypes); every entry point returns int status except the string getters.
 _P = ctypes.POINTER(CtgbParams)
 _vp, _i32, _f32, _sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_float, ctypes.c_size_t
@@ -102,6 +122,12 @@ SIGNATURES = {
     "ctgb_fan_batch_bytes": [ctypes.POINTER(CtgbFanSlice), _i32, _i32, _i32, ctypes.POINTER(_sz)],
     "ctgb_fan_batch_build": [ctypes.POINTER(CtgbFanSlice), _i32, _i32, _i32, _vp, _sz],
     "ctgb_fan_backproject": [_vp, _i32, _vp, _vp, _i32, _i32, _i32, _i32, _vp],
+    "ctgb_batch_forward_plan_bytes": [ctypes.POINTER(CtgbFwdJob), _i32, ctypes.POINTER(_sz)],
+    "ctgb_batch_forward_plan": [ctypes.POINTER(CtgbFwdJob), _i32, _vp, _sz],
+    "ctgb_batch_forward": [_vp, _vp, _i32, _vp],
+    "ctgb_batch_backproject_plan_bytes": [ctypes.POINTER(CtgbBpJob), _i32, ctypes.POINTER(_sz)],
+    "ctgb_batch_backproject_plan": [ctypes.POINTER(CtgbBpJob), _i32, _i32, _vp, _sz],
+    "ctgb_batch_backproject": [_vp, _vp, _i32, _vp],
 }
 STRING_FUNCS = ("ctgb_last_error", "ctgb_version")
 

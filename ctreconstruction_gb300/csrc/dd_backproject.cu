@@ -27,9 +27,13 @@
 //    voxel receives is bit-for-bit the weight the forward gives it.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
+
 #include "dd_common.cuh"
 #include "status.h"
 #include "tma.cuh"
+#include "updates.cuh"
 
 namespace ctgb {
 
@@ -253,10 +257,9 @@ constexpr int kBiBlocks = CTGB_BI_BLOCKS;   // resident CTAs per SM the register
 constexpr int kBiTX = CTGB_BI_TX, kBiTY = CTGB_BI_TY;
 static_assert(kBiTX * kBiTY == 128 && 32 % kBiTX == 0, "bp_fdk_integ_kernel: 128-thread CTAs of whole warps");
 
-__global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__restrict__ out, int nu, int nv,
-                                      int nviews) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)nu * nviews) return;
+// Column l of view v (t = v * nu + l): running sums C(m) next to the values.
+__device__ __forceinline__ void integrate_rows_one(const float *__restrict__ proj, float2 *__restrict__ out, int nu,
+                                                   int nv, long long t) {
     const int v = (int)(t / nu), l = (int)(t % nu);
     const float *__restrict__ q = proj + (long long)v * nu * nv + l;
     float2 *__restrict__ o = out + (long long)v * (nv + 1) * nu + l;
@@ -267,6 +270,13 @@ __global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__
         c += x;
     }
     o[(long long)nv * nu] = make_float2((float)c, 0.0f);
+}
+
+__global__ void integrate_rows_kernel(const float *__restrict__ proj, float2 *__restrict__ out, int nu, int nv,
+                                      int nviews) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * nviews) return;
+    integrate_rows_one(proj, out, nu, nv, t);
 }
 
 template <int NT>
@@ -338,19 +348,77 @@ __device__ __forceinline__ void integ_dispatch(bool clamp, const float2 *__restr
                                         imax, Mv, Av, acc);
 }
 
-template <bool CURVED>
-__global__ void __launch_bounds__(kBiTX * kBiTY, kBiBlocks)
-bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ, float *__restrict__ vol,
-                    int view0, int nviews, float scale, int accumulate) {
-    const TableHeader &h = header(T);
-    const int ix = blockIdx.x * kBiTX + threadIdx.x;
-    const int iy = blockIdx.y * kBiTY + threadIdx.y;
-    const int z0 = blockIdx.z * kBiZ;
-    const bool live = ix < h.nx && iy < h.ny;
-    const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
+// Per-launch values of a backprojection (table, integrated projections,
+// views, scale).  The single-scan kernels take them from their parameters,
+// which the column bodies can read at any use for free.  The batched kernels
+// read them from the job in global memory: JobSrc re-loads a field at every
+// use (a volatile load is not hoisted out of the view loop), so the seven
+// values are not held in registers across it — held there, they pushed the
+// column bodies' accumulators into local memory (732-byte spills).
+struct ParamSrc {
+    const float *T_;
+    const float2 *integ_;
+    const float *tabs_, *proj_;
+    int view0_, nviews_;
+    float scale_;
+    __device__ __forceinline__ const float *T() const { return T_; }
+    __device__ __forceinline__ const float2 *integ() const { return integ_; }
+    __device__ __forceinline__ const float *tabs() const { return tabs_; }
+    __device__ __forceinline__ const float *proj() const { return proj_; }
+    __device__ __forceinline__ int view0() const { return view0_; }
+    __device__ __forceinline__ int nviews() const { return nviews_; }
+    __device__ __forceinline__ float scale() const { return scale_; }
+};
+
+__device__ __forceinline__ unsigned long long ld_volatile_u64(const void *p) {
+    unsigned long long v;
+    asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ unsigned ld_volatile_u32(const void *p) {
+    unsigned v;
+    asm volatile("ld.global.nc.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+template <class Job>
+struct JobSrc {
+    const Job *jp;
+    __device__ __forceinline__ const float *T() const { return reinterpret_cast<const float *>(ld_volatile_u64(&jp->T)); }
+    __device__ __forceinline__ const float2 *integ() const {
+        return reinterpret_cast<const float2 *>(ld_volatile_u64(&jp->integ));
+    }
+    __device__ __forceinline__ const float *tabs() const {
+        return reinterpret_cast<const float *>(ld_volatile_u64(&jp->tabs));
+    }
+    __device__ __forceinline__ const float *proj() const {
+        return reinterpret_cast<const float *>(ld_volatile_u64(&jp->proj));
+    }
+    __device__ __forceinline__ int view0() const { return (int)ld_volatile_u32(&jp->view0); }
+    __device__ __forceinline__ int nviews() const { return (int)ld_volatile_u32(&jp->nviews); }
+    __device__ __forceinline__ float scale() const { return __uint_as_float(ld_volatile_u32(&jp->scale)); }
+};
+
+// CTA (bx, by, bz) of the FDK backprojection over integrated projections:
+// the body of the single-scan and the batched kernels.  store(i, b) writes
+// the result b of volume index i (a plain store, or an iterate's update); it
+// fetches its own operands, so nothing it needs is held in registers across
+// the view loop.
+template <bool CURVED, class Src, class Store>
+__device__ __forceinline__ void bp_fdk_column(const Src &src, int bx, int by, int bz, Store store) {
+    const float *__restrict__ T0 = src.T();
+    const TableHeader &h0 = header(T0);
+    const int ix = bx * kBiTX + threadIdx.x;
+    const int iy = by * kBiTY + threadIdx.y;
+    const int z0 = bz * kBiZ;
+    const bool live = ix < h0.nx && iy < h0.ny;
+    const int nxh = h0.nx, nyh = h0.ny;
+    const int ixc = min(ix, h0.nx - 1), iyc = min(iy, h0.ny - 1);
+    const int nu = h0.nu, nv = h0.nv, nz = h0.nz;
+#define T T0
+#define h h0
     const float *__restrict__ ki = T + h.off_ki;
     const float *__restrict__ pp = T + h.off_pp;
-    const int nu = h.nu, nv = h.nv, nz = h.nz;
     const float xx = T[h.off_xpix + ixc], yy = T[h.off_ypix + iyc];
     const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f, dzs = h.dz;
     const float du = h.du_bp, dv = h.dv_bp, inv_du = 1.0f / du, inv_dv = 1.0f / dv;
@@ -361,14 +429,21 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
     const int zlast = min(z0 + kBiZ, nz) - 1 - z0;
     const float zend = zfirst + (float)zlast * dzs;
     const float inv_zlast = zlast > 0 ? 1.0f / (float)zlast : 0.0f;
+#undef T
+#undef h
     float acc[kBiZ];
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) acc[j] = 0.0f;
 
-    for (int vi = 0; vi < nviews; ++vi) {
-        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
+    for (int vi = 0; vi < src.nviews(); ++vi) {
+        const float *__restrict__ T = src.T();
+        const TableHeader &h = header(T);
+        const float *__restrict__ ki = T + h.off_ki;
+        const float *__restrict__ pp = T + h.off_pp;
+        const float *__restrict__ V = T + h.off_views + (long long)(src.view0() + vi) * h.view_stride;
         const float cs = V[VF_COS], sn = V[VF_SIN], Sz = V[VF_BPSZ];
-        const float2 *__restrict__ IQ = integ + (long long)vi * (nv + 1) * nu;
+        const float2 *__restrict__ IQ = src.integ() + (long long)vi * (nv + 1) * nu;
+        const float scale = src.scale();
         const float yc = yy * cs - xx * sn;
         float umin = INFINITY, umax = -INFINITY, imin = INFINITY, imax = -INFINITY;
 #pragma unroll
@@ -490,11 +565,17 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
 #pragma unroll
     for (int j = 0; j < kBiZ; ++j) {
         const int iz = z0 + j;
-        if (iz < nz) {
-            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
-            *dst = accumulate ? *dst + acc[j] : acc[j];
-        }
+        if (iz < nz) store(((long long)iz * nyh + iy) * nxh + ix, acc[j]);
     }
+}
+
+template <bool CURVED>
+__global__ void __launch_bounds__(kBiTX * kBiTY, kBiBlocks)
+bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ, float *__restrict__ vol,
+                    int view0, int nviews, float scale, int accumulate) {
+    const ParamSrc src = {T, integ, nullptr, nullptr, view0, nviews, scale};
+    bp_fdk_column<CURVED>(src, blockIdx.x, blockIdx.y, blockIdx.z,
+                          [=](long long i, float b) { vol[i] = accumulate ? __fadd_rn(vol[i], b) : b; });
 }
 
 // ---- matched (adjoint) backprojector ---------------------------------------
@@ -704,13 +785,13 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
 // instead of dividing per voxel column (the search was most of its time).
 __device__ __forceinline__ int matched_tab_stride(int nu) { return 2 * nu + 2; }
 
-__global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
-                                         float2 *__restrict__ out, float *__restrict__ tabs, int view0,
-                                         int nviews) {
+// Column c of view vi (t = vi * nu + c) of the matched backprojector's
+// integration pass.
+__device__ __forceinline__ void matched_integrate_one(const float *__restrict__ T, const float *__restrict__ proj,
+                                                      float2 *__restrict__ out, float *__restrict__ tabs, int view0,
+                                                      long long t) {
     const TableHeader &h = header(T);
     const int nu = h.nu, nv = h.nv;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)nu * nviews) return;
     const int vi = (int)(t / nu), c = (int)(t % nu);
     const ViewOffsets vo = view_offsets(nu, nv);
     const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
@@ -753,6 +834,14 @@ __global__ void matched_integrate_kernel(const float *__restrict__ T, const floa
     o[(long long)nv * nu] = make_float2((float)run, 0.0f);
 }
 
+__global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
+                                         float2 *__restrict__ out, float *__restrict__ tabs, int view0,
+                                         int nviews) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)header(T).nu * nviews) return;
+    matched_integrate_one(T, proj, out, tabs, view0, t);
+}
+
 constexpr int kMC = 6;   // detector columns kept per (voxel column, view); more -> per-voxel path
 
 #ifndef CTGB_MI_BLOCKS
@@ -770,30 +859,34 @@ constexpr int kMC = 6;   // detector columns kept per (voxel column, view); more
 constexpr int kMiTX = CTGB_MI_TX, kMiTY = CTGB_MI_TY;
 static_assert(kMiTX * kMiTY == 128 && 32 % kMiTX == 0, "bp_matched_integ_kernel: 128-thread CTAs of whole warps");
 
-__global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MI_BLOCKS)
-bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
-                        const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
-                        int view0, int nviews, float scale, int accumulate) {
-    const TableHeader &h = header(T);
-    const int ix = blockIdx.x * kMiTX + threadIdx.x;
-    const int iy = blockIdx.y * kMiTY + threadIdx.y;
-    const int l0 = blockIdx.z * kMZ;
+// CTA (bx, by, bz) of the matched backprojection over prescaled, integrated
+// projections: the body of the single-scan and the batched kernels; store as
+// for bp_fdk_column (it receives A^T r before the scale).
+template <class Src, class Store>
+__device__ __forceinline__ void bp_matched_column(const Src &src, int bx, int by, int bz, Store store) {
+    const TableHeader &h = header(src.T());
+    const int ix = bx * kMiTX + threadIdx.x;
+    const int iy = by * kMiTY + threadIdx.y;
+    const int l0 = bz * kMZ;
     const bool live = ix < h.nx && iy < h.ny;
     const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
     const int nu = h.nu, nv = h.nv, nz = h.nz;
     const ViewOffsets vo = view_offsets(nu, nv);
-    const float *__restrict__ pzp = T + h.off_zplane;
     const float inv_dz = 1.0f / h.dz;
     const float fnv = (float)nv;
+    const int nxh = h.nx, nyh = h.ny;
     float acc[kMZ];
 #pragma unroll
     for (int j = 0; j < kMZ; ++j) acc[j] = 0.0f;
 
-    for (int vi = 0; vi < nviews; ++vi) {
-        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
-        const float2 *__restrict__ IQ = integ + (long long)vi * (nv + 1) * nu;
+    for (int vi = 0; vi < src.nviews(); ++vi) {
+        const float *__restrict__ T = src.T();
+        const TableHeader &h = header(T);
+        const float *__restrict__ pzp = T + h.off_zplane;
+        const float *__restrict__ V = T + h.off_views + (long long)(src.view0() + vi) * h.view_stride;
+        const float2 *__restrict__ IQ = src.integ() + (long long)vi * (nv + 1) * nu;
         const int axis = (int)V[VF_AXIS];
-        const float *__restrict__ Qraw = proj + (long long)vi * nu * nv;
+        const float *__restrict__ Qraw = src.proj() + (long long)vi * nu * nv;
         if (axis == 2) {
             // z-dominant: per-voxel candidate search on the raw values.
             if (!live) continue;
@@ -830,7 +923,7 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
         const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
         const float kf = (float)k;
         // Up to kMC columns with ov_x > 0 (the same x' expressions as the forward).
-        const float *__restrict__ EbT = tabs + (long long)vi * matched_tab_stride(nu);
+        const float *__restrict__ EbT = src.tabs() + (long long)vi * matched_tab_stride(nu);
         const float *__restrict__ IPT = EbT + nu + 1;
         int ncol = 0;
         int cc[kMC];
@@ -904,10 +997,97 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
 #pragma unroll
     for (int j = 0; j < kMZ; ++j) {
         const int iz = l0 + j;
-        if (iz < nz) {
-            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
-            *dst = accumulate ? *dst + scale * acc[j] : scale * acc[j];
+        if (iz < nz) store(((long long)iz * nyh + iy) * nxh + ix, acc[j]);
+    }
+}
+
+__global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MI_BLOCKS)
+bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
+                        const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
+                        int view0, int nviews, float scale, int accumulate) {
+    const ParamSrc src = {T, integ, tabs, proj, view0, nviews, scale};
+    bp_matched_column(src, blockIdx.x, blockIdx.y, blockIdx.z,
+                      [=](long long i, float a) {
+                          const float b = __fmul_rn(scale, a);
+                          vol[i] = accumulate ? __fadd_rn(vol[i], b) : b;
+                      });
+}
+
+// ---- batched backprojection (many scans per launch) --------------------------
+// Job j covers the CTA items [item0, item0 + gx * gy * gz) of its scan's grid
+// (x fastest); the integration pass covers threads [t0, t0 + nu * nviews).
+struct BpJob {
+    const float *T;
+    const float2 *integ;        // integrated projections of the job's views
+    const float *tabs;          // matched: the per-view column tables after them
+    const float *proj;          // raw projections (matched: z-dominant views and wide footprints)
+    float *vol;
+    int view0, nviews;
+    float scale;
+    int accumulate;
+    int gx, gy, gz, item0;
+    BpEpi epi;
+};
+
+struct IntegJob {
+    const float *T;
+    const float *proj;
+    float2 *out;
+    float *tabs;
+    int view0, nu, nv, pad;
+    long long t0;
+};
+
+// The batched bodies need more registers than the single-scan ones (at eight
+// or six CTAs per SM they spilled 700 and 270 bytes): four CTAs per SM.
+constexpr int kBatchBpBlocks = 4;
+
+template <bool CURVED>
+__global__ void __launch_bounds__(kBiTX * kBiTY, kBatchBpBlocks)
+bp_fdk_batch_kernel(const BpJob *__restrict__ jobs, int njobs, int nitems) {
+    int j = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        while (j + 1 < njobs && it >= jobs[j + 1].item0) ++j;
+        const BpJob &jb = jobs[j];
+        const int local = it - jb.item0, gxy = jb.gx * jb.gy;
+        const int bz = local / gxy, r = local - bz * gxy;
+        const BpJob *jp = jobs + j;
+        const JobSrc<BpJob> src = {jp};
+        bp_fdk_column<CURVED>(src, r % jb.gx, r / jb.gx, bz,
+                              [=](long long i, float b) { bp_epilogue(jp->epi, jp->vol, i, b, jp->accumulate); });
+    }
+}
+
+__global__ void __launch_bounds__(kMiTX * kMiTY, kBatchBpBlocks)
+bp_matched_batch_kernel(const BpJob *__restrict__ jobs, int njobs, int nitems) {
+    int j = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        while (j + 1 < njobs && it >= jobs[j + 1].item0) ++j;
+        const BpJob &jb = jobs[j];
+        const int local = it - jb.item0, gxy = jb.gx * jb.gy;
+        const int bz = local / gxy, r = local - bz * gxy;
+        const BpJob *jp = jobs + j;
+        const JobSrc<BpJob> src = {jp};
+        bp_matched_column(src, r % jb.gx, r / jb.gx, bz,
+                          [=](long long i, float a) {
+                              bp_epilogue(jp->epi, jp->vol, i, __fmul_rn(jp->scale, a), jp->accumulate);
+                          });
+    }
+}
+
+template <bool MATCHED>
+__global__ void integrate_batch_kernel(const IntegJob *__restrict__ jobs, int njobs, long long nthreads) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nthreads;
+         t += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = njobs - 1;   // last job with t0 <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].t0 <= t) lo = mid;
+            else hi = mid - 1;
         }
+        const IntegJob &jb = jobs[lo];
+        if (MATCHED) matched_integrate_one(jb.T, jb.proj, jb.out, jb.tabs, jb.view0, t - jb.t0);
+        else integrate_rows_one(jb.proj, jb.out, jb.nu, jb.nv, t - jb.t0);
     }
 }
 
@@ -1121,5 +1301,165 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_integ_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+namespace {
+
+constexpr uint32_t kBpPlanMagic = 0x31425042u;
+
+// Host and device copies of a plan are the same bytes: this head, the BpJob
+// array, the IntegJob array.
+struct BpPlanHead {
+    uint32_t magic;
+    int32_t matched, curved, njobs;
+    int32_t nitems, pad;
+    int64_t nthreads, off_jobs, off_integ, total;
+};
+
+size_t bp_align(size_t v) { return (v + 127) / 128 * 128; }
+
+int build_bp_plan(const ctgb_bp_job *jobs, int njobs, int matched, unsigned char *out, size_t bytes, size_t *need) {
+    if (!jobs || njobs < 1) return set_error(CTGB_ERR_ARG, "batched backprojection: no jobs");
+    int curved = -1;
+    long long items = 0, threads = 0;
+    for (int i = 0; i < njobs; ++i) {
+        const ctgb_bp_job &jb = jobs[i];
+        const ctgb_params *p = jb.params;
+        if (!p || !jb.table || !jb.workspace || (!jb.proj && jb.nviews > 0))
+            return set_error(CTGB_ERR_ARG, "batched backprojection: job %d has a NULL argument", i);
+        if (jb.view0 < 0 || jb.nviews < 0 || jb.view0 + jb.nviews > p->nviews)
+            return set_error(CTGB_ERR_ARG, "batched backprojection: job %d view range outside the scan", i);
+        if (jb.epilogue < CTGB_BP_STORE || jb.epilogue > CTGB_BP_POCS_UPDATE)
+            return set_error(CTGB_ERR_ARG, "batched backprojection: job %d unknown epilogue %d", i, jb.epilogue);
+        if (jb.epilogue == CTGB_BP_STORE ? !jb.vol : (!jb.x || !jb.n1))
+            return set_error(CTGB_ERR_ARG, "batched backprojection: job %d epilogue output missing", i);
+        if (!matched && p->nu < 4)
+            return set_error(CTGB_ERR_ARG, "batched backprojection: job %d has fewer than 4 detector columns", i);
+        size_t ws = 0;
+        if (int st = ctgb_backproject_fdk_workspace_bytes(p, jb.nviews, &ws)) return st;
+        if (jb.workspace_bytes < ws)
+            return set_error(CTGB_ERR_SIZE, "batched backprojection: job %d workspace of %zu bytes below %zu", i,
+                             jb.workspace_bytes, ws);
+        if (!matched) {
+            if (curved >= 0 && curved != (p->curved ? 1 : 0))
+                return set_error(CTGB_ERR_ARG, "batched backprojection: flat and curved detectors in one plan");
+            curved = p->curved ? 1 : 0;
+        }
+        const int tx = matched ? kMiTX : kBiTX, ty = matched ? kMiTY : kBiTY, tz = matched ? kMZ : kBiZ;
+        items += (long long)((p->nx + tx - 1) / tx) * ((p->ny + ty - 1) / ty) * ((p->nz + tz - 1) / tz);
+        threads += (long long)p->nu * jb.nviews;
+    }
+    if (items > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "batched backprojection: too many blocks");
+    BpPlanHead head;
+    std::memset(&head, 0, sizeof head);
+    head.magic = kBpPlanMagic;
+    head.matched = matched ? 1 : 0;
+    head.curved = curved > 0 ? 1 : 0;
+    head.njobs = njobs;
+    head.nitems = (int32_t)items;
+    head.nthreads = threads;
+    head.off_jobs = (int64_t)bp_align(sizeof head);
+    head.off_integ = (int64_t)bp_align(head.off_jobs + sizeof(BpJob) * njobs);
+    head.total = (int64_t)bp_align(head.off_integ + sizeof(IntegJob) * njobs);
+    *need = (size_t)head.total;
+    if (!out) return CTGB_OK;
+    if (bytes < *need)
+        return set_error(CTGB_ERR_SIZE, "batched backprojection: plan buffer of %zu bytes below %zu", bytes, *need);
+    std::memset(out, 0, *need);
+    std::memcpy(out, &head, sizeof head);
+    BpJob *bj = reinterpret_cast<BpJob *>(out + head.off_jobs);
+    IntegJob *ij = reinterpret_cast<IntegJob *>(out + head.off_integ);
+    int item = 0;
+    long long t0 = 0;
+    for (int i = 0; i < njobs; ++i) {
+        const ctgb_bp_job &jb = jobs[i];
+        const ctgb_params *p = jb.params;
+        float2 *ws = static_cast<float2 *>(jb.workspace);
+        float *tabs = reinterpret_cast<float *>(ws + (size_t)jb.nviews * (p->nv + 1) * p->nu);
+        BpJob &b = bj[i];
+        b.T = static_cast<const float *>(jb.table);
+        b.integ = ws;
+        b.tabs = tabs;
+        b.proj = jb.proj;
+        b.vol = jb.vol;
+        b.view0 = jb.view0;
+        b.nviews = jb.nviews;
+        b.scale = jb.scale;
+        b.accumulate = jb.accumulate ? 1 : 0;
+        const int tx = matched ? kMiTX : kBiTX, ty = matched ? kMiTY : kBiTY, tz = matched ? kMZ : kBiZ;
+        b.gx = (p->nx + tx - 1) / tx;
+        b.gy = (p->ny + ty - 1) / ty;
+        b.gz = (p->nz + tz - 1) / tz;
+        b.item0 = item;
+        item += b.gx * b.gy * b.gz;
+        b.epi.mode = jb.epilogue;
+        b.epi.coef = jb.coef;
+        b.epi.eps = jb.eps;
+        b.epi.x = jb.x;
+        b.epi.n1 = jb.n1;
+        IntegJob &g = ij[i];
+        g.T = b.T;
+        g.proj = jb.proj;
+        g.out = ws;
+        g.tabs = tabs;
+        g.view0 = jb.view0;
+        g.nu = p->nu;
+        g.nv = p->nv;
+        g.t0 = t0;
+        t0 += (long long)p->nu * jb.nviews;
+    }
+    return CTGB_OK;
+}
+
+}  // namespace
+
+extern "C" int ctgb_batch_backproject_plan_bytes(const ctgb_bp_job *jobs, int32_t njobs, size_t *bytes) {
+    clear_error();
+    if (!bytes) return set_error(CTGB_ERR_ARG, "ctgb_batch_backproject_plan_bytes: NULL argument");
+    // the layout does not depend on the backprojector kind
+    return build_bp_plan(jobs, njobs, 1, nullptr, 0, bytes);
+}
+
+extern "C" int ctgb_batch_backproject_plan(const ctgb_bp_job *jobs, int32_t njobs, int32_t matched, void *host_plan,
+                                           size_t bytes) {
+    clear_error();
+    if (!host_plan) return set_error(CTGB_ERR_ARG, "ctgb_batch_backproject_plan: NULL plan");
+    size_t need = 0;
+    return build_bp_plan(jobs, njobs, matched, static_cast<unsigned char *>(host_plan), bytes, &need);
+}
+
+extern "C" int ctgb_batch_backproject(const void *host_plan, const void *d_plan, int32_t ctas_per_sm, void *stream) {
+    clear_error();
+    if (!host_plan || !d_plan || ctas_per_sm < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_batch_backproject: bad arguments");
+    const BpPlanHead &head = *static_cast<const BpPlanHead *>(host_plan);
+    if (head.magic != kBpPlanMagic) return set_error(CTGB_ERR_ARG, "ctgb_batch_backproject: not a backprojection plan");
+    if (reinterpret_cast<uintptr_t>(d_plan) % 128)
+        return set_error(CTGB_ERR_ARG, "ctgb_batch_backproject: device plan must be 128-byte aligned");
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "ctgb_batch_backproject: %s", cudaGetErrorString(e));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned char *dp = static_cast<const unsigned char *>(d_plan);
+    const IntegJob *ij = reinterpret_cast<const IntegJob *>(dp + head.off_integ);
+    const BpJob *bj = reinterpret_cast<const BpJob *>(dp + head.off_jobs);
+    if (head.nthreads > 0) {
+        const long long blocks = std::min<long long>((head.nthreads + 255) / 256, (long long)sms * 8);
+        if (head.matched) integrate_batch_kernel<true><<<(unsigned)blocks, 256, 0, st>>>(ij, head.njobs, head.nthreads);
+        else integrate_batch_kernel<false><<<(unsigned)blocks, 256, 0, st>>>(ij, head.njobs, head.nthreads);
+    }
+    if (head.nitems > 0) {
+        const int grid = (int)std::min<long long>(head.nitems, (long long)sms * ctas_per_sm);
+        if (head.matched)
+            bp_matched_batch_kernel<<<grid, dim3(kMiTX, kMiTY), 0, st>>>(bj, head.njobs, head.nitems);
+        else if (head.curved)
+            bp_fdk_batch_kernel<true><<<grid, dim3(kBiTX, kBiTY), 0, st>>>(bj, head.njobs, head.nitems);
+        else
+            bp_fdk_batch_kernel<false><<<grid, dim3(kBiTX, kBiTY), 0, st>>>(bj, head.njobs, head.nitems);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "batched backprojection: %s", cudaGetErrorString(e));
     return CTGB_OK;
 }

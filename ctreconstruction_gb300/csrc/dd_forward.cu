@@ -25,6 +25,7 @@
 #include "dd_common.cuh"
 #include "status.h"
 #include "tma.cuh"
+#include "updates.cuh"
 
 namespace ctgb {
 
@@ -98,10 +99,10 @@ dd_forward_kernel(const float *__restrict__ T, const float *__restrict__ vol, co
     proj[((long long)vi * h.nv + r) * h.nu + c] = val;
 }
 
-__global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny) {
-    __shared__ float tile[32][33];
-    const int z = blockIdx.z;
-    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+// One 32 x 32 tile (bx, by) of slice z of the [z][y][x] -> [z][x][y] copy.
+__device__ __forceinline__ void transpose_tile(float (&tile)[32][33], const float *__restrict__ in,
+                                               float *__restrict__ out, int nx, int ny, int bx, int by, int z) {
+    const int x0 = bx * 32, y0 = by * 32;
     const float *src = in + (long long)z * nx * ny;
     float *dst = out + (long long)z * nx * ny;
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
@@ -112,6 +113,31 @@ __global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restr
     for (int j = threadIdx.y; j < 32; j += blockDim.y) {
         int y = y0 + threadIdx.x, x = x0 + j;
         if (x < nx && y < ny) dst[(long long)x * ny + y] = tile[threadIdx.x][j];
+    }
+}
+
+__global__ void transpose_xy_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny) {
+    __shared__ float tile[32][33];
+    transpose_tile(tile, in, out, nx, ny, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// Batched transpose: job j's tiles are items item0 .. item0 + tx * ty * nz - 1.
+struct TransJob {
+    const float *in;
+    float *out;
+    int nx, ny, nz, tx, ty, item0;
+};
+
+__global__ void transpose_xy_batch_kernel(const TransJob *__restrict__ jobs, int njobs, int nitems) {
+    __shared__ float tile[32][33];
+    int j = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        while (j + 1 < njobs && it >= jobs[j + 1].item0) ++j;
+        const TransJob &jb = jobs[j];
+        const int local = it - jb.item0, per = jb.tx * jb.ty;
+        const int z = local / per, t = local - z * per;
+        transpose_tile(tile, jb.in, jb.out, jb.nx, jb.ny, t % jb.tx, t / jb.tx, z);
+        __syncthreads();   // the tile is rewritten by the next item
     }
 }
 
@@ -282,18 +308,36 @@ struct FwdViewList {
     int v[kFwdListViews];
 };
 
-template <bool XD, bool TMA, int TR>
-__global__ void __launch_bounds__(32, FwdTile<TR>::MINB)
-dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
-                      const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0,
-                      const __grid_constant__ FwdViewList views, int ntu, int *status) {
-    extern __shared__ __align__(128) unsigned char smraw[];
+// Barriers initialised and patch buffers zeroed once per CTA (taps past the
+// loaded boxes then read finite zeros).
+template <int TR>
+__device__ __forceinline__ void fwd_smem_init(FwdTmaSmem<TR> &sm) {
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+        mbar_init(&sm.bar[0], 1);
+        mbar_init(&sm.bar[1], 1);
+        fence_mbar_init();
+    }
+    float4 *z = reinterpret_cast<float4 *>(&sm.buf[0][0][0]);
+    for (int i = lane; i < kFwdBufs * FwdTile<TR>::PZ * kPX / 4; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+}
+
+// One detector tile (kTU columns x TR rows, tile (tu, tv)) of view vi
+// (relative to view0): the body of the single-scan and the batched forward
+// kernels.  phase_bits carries the barriers' phases from tile to tile; every
+// copy a tile issues is consumed before it returns.  The stored value goes
+// through the epilogue epi (the projection itself, or an iterative
+// driver's residual).  Returns false when a bounded wait ran out (the
+// tile's copies drained first).
+template <bool XD, int TR>
+__device__ __forceinline__ bool fwd_tile(FwdTmaSmem<TR> &sm, const CUtensorMap *tmp, bool TMA,
+                                         const float *__restrict__ T, const float *__restrict__ src, long long st_k,
+                                         float *__restrict__ proj, int view0, int vi, int tu, int tv,
+                                         const FwdEpi &epi, uint32_t &phase_bits, int *status) {
     constexpr int kTR = TR, kPZ = FwdTile<TR>::PZ;
-    FwdTmaSmem<TR> &sm = *reinterpret_cast<FwdTmaSmem<TR> *>(smraw);
     const TableHeader &h = header(T);
     const int lane = threadIdx.x;
-    const int vi = views.v[blockIdx.x];           // view index relative to view0
-    const int tu = blockIdx.y % ntu, tv = blockIdx.y / ntu;
     const int c0 = tu * kTU, r0 = tv * kTR;
     const int nu = h.nu, nv = h.nv;
     const ViewOffsets vo = view_offsets(nu, nv);
@@ -353,22 +397,10 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         return w;
     };
 
-    if (lane == 0) {
-        mbar_init(&sm.bar[0], 1);
-        mbar_init(&sm.bar[1], 1);
-        fence_mbar_init();
-    }
-    // Zero both buffers once so that taps past the loaded boxes read finite zeros.
-    {
-        float4 *z = reinterpret_cast<float4 *>(&sm.buf[0][0][0]);
-        for (int i = lane; i < kFwdBufs * kPZ * kPX / 4; i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    __syncwarp();
-
     float2 acc[kTR / 2];   // rows j (.x) and kTR / 2 + j (.y)
 #pragma unroll
     for (int j = 0; j < kTR / 2; ++j) acc[j] = make_float2(0.0f, 0.0f);
-    uint32_t phase_bits = 0u, pending_bits = 0u;   // bit b: phase parity / TMA outstanding for buffer b
+    uint32_t pending_bits = 0u;   // bit b: TMA outstanding for buffer b (phase_bits: its phase parity)
     bool failed = false;
 
     auto issue = [&](int s, const TileWindow &w, int b) {
@@ -376,7 +408,7 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         if (lane == 0) {
             mbar_arrive_expect_tx(&sm.bar[b], (uint32_t)(w.nbz * kBoxZ * kBoxX * 4));
             for (int iz = 0; iz < w.nbz; ++iz)
-                tma_load_3d(&sm.buf[b][iz * kBoxZ][0], &tm, w.kb, s, w.lb + iz * kBoxZ, &sm.bar[b]);
+                tma_load_3d(&sm.buf[b][iz * kBoxZ][0], tmp, w.kb, s, w.lb + iz * kBoxZ, &sm.bar[b]);
         }
         pending_bits |= 1u << b;
     };
@@ -468,9 +500,9 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         // Let copies still in flight land before the CTA exits (bounded).
         for (int b = 0; b < kFwdBufs; ++b)
             if ((pending_bits >> b) & 1u) mbar_wait(&sm.bar[b], (phase_bits >> b) & 1u, status);
-        return;
+        return false;
     }
-    if (c >= nu) return;
+    if (c >= nu) return true;
     const float dEb = fabsf(Eb1 - Eb0);
     const float absInvD = fabsf(invD);
     const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (dEb * absInvD);
@@ -480,8 +512,60 @@ dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__res
         if (r < nv) {
             const float t2 = (Sz - Pzr[r]) * invD;
             const float K = base * sqrtf(1.0f + t2 * t2) / rowspan_max;
-            proj[((long long)vi * nv + r) * nu + c] = (j < kTR / 2 ? acc[j].x : acc[j - kTR / 2].y) * K;
+            const long long i = ((long long)vi * nv + r) * nu + c;
+            proj[i] = fwd_epilogue(epi, i, (j < kTR / 2 ? acc[j].x : acc[j - kTR / 2].y) * K);
         }
+    }
+    return true;
+}
+
+template <bool XD, bool TMA, int TR>
+__global__ void __launch_bounds__(32, FwdTile<TR>::MINB)
+dd_forward_tma_kernel(const __grid_constant__ CUtensorMap tm, const float *__restrict__ T,
+                      const float *__restrict__ src, long long st_k, float *__restrict__ proj, int view0,
+                      const __grid_constant__ FwdViewList views, int ntu, int *status) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    FwdTmaSmem<TR> &sm = *reinterpret_cast<FwdTmaSmem<TR> *>(smraw);
+    fwd_smem_init<TR>(sm);
+    uint32_t phase_bits = 0u;
+    const FwdEpi epi = {kFwdStore, 0.0f, nullptr, nullptr};
+    fwd_tile<XD, TR>(sm, &tm, TMA, T, src, st_k, proj, view0, views.v[blockIdx.x], blockIdx.y % ntu,
+                     blockIdx.y / ntu, epi, phase_bits, status);
+}
+
+// Batched forward: the views of many scans (one axis, one tile height) in one
+// persistent launch.  Job j covers items [item0, item0 + nitems): view
+// views[list0 + k] (relative to the job's view0) x tile t for item
+// item0 + k * ntiles + t.  Each CTA walks items blockIdx.x, + gridDim.x, ...
+// in increasing order, so its job index only moves forward.
+struct __align__(128) FwdJob {
+    CUtensorMap tm;            // the scan's volume ([z][x][y] copy for x-dominant views) as a TMA tensor
+    const float *T;            // geometry table
+    const float *src;          // the volume layout the kernel reads
+    float *proj;               // output of views view0 .. view0 + nviews - 1 (projections or residual)
+    long long st_k;            // 1: x-dominant views read the [z][x][y] copy
+    int view0, ntu, ntiles, tma;
+    int item0, nitems, list0, pad;
+    FwdEpi epi;
+};
+
+template <bool XD, int TR>
+__global__ void __launch_bounds__(32, FwdTile<TR>::MINB)
+dd_forward_batch_kernel(const FwdJob *__restrict__ jobs, int njobs, const int *__restrict__ views, int nitems,
+                        int *status) {
+    extern __shared__ __align__(128) unsigned char smraw[];
+    FwdTmaSmem<TR> &sm = *reinterpret_cast<FwdTmaSmem<TR> *>(smraw);
+    fwd_smem_init<TR>(sm);
+    uint32_t phase_bits = 0u;
+    int j = 0;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        while (j + 1 < njobs && it >= jobs[j + 1].item0) ++j;
+        const FwdJob &jb = jobs[j];
+        const int local = it - jb.item0;
+        const int k = local / jb.ntiles, t = local - k * jb.ntiles;
+        if (!fwd_tile<XD, TR>(sm, &jb.tm, jb.tma != 0, jb.T, jb.src, jb.st_k, jb.proj, jb.view0,
+                              views[jb.list0 + k], t % jb.ntu, t / jb.ntu, jb.epi, phase_bits, status))
+            return;
     }
 }
 
@@ -678,4 +762,229 @@ extern "C" int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t n
     dim3 grid((nx + 31) / 32, (ny + 31) / 32, nz), block(32, 8);
     transpose_xy_kernel<<<grid, block, 0, static_cast<cudaStream_t>(stream)>>>(d_vol, d_vol_xzy, nx, ny);
     return check_launch("transpose_xy_kernel");
+}
+
+// ---- batched forward (many scans per launch) ---------------------------------
+namespace {
+
+constexpr uint32_t kFwdPlanMagic = 0x31424643u;
+
+struct FwdPlanGroup {
+    int32_t xd, tr, njobs, nitems;
+    int64_t off_jobs, off_views;
+};
+
+// Host and device copies of a plan are the same bytes: this head, then per
+// group its FwdJob array (128-byte aligned, as CUtensorMap) and view list,
+// then the TransJobs.
+struct FwdPlanHead {
+    uint32_t magic;
+    int32_t ngroups;
+    int32_t ntrans, trans_items;
+    int64_t off_trans, total;
+    FwdPlanGroup g[4];
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+int device_sms(int *sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "SM count: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
+// Lays the plan out (and fills it when out != nullptr).
+int build_fwd_plan(const ctgb_fwd_job *jobs, int njobs, unsigned char *out, size_t bytes, size_t *need) {
+    if (!jobs || njobs < 1) return set_error(CTGB_ERR_ARG, "batched forward: no jobs");
+    struct Scan {
+        int tr, ntu, ntiles;
+        std::vector<int> views[2];   // [0] x-dominant, [1] y-dominant (relative view indices)
+    };
+    std::vector<Scan> sc(njobs);
+    for (int i = 0; i < njobs; ++i) {
+        const ctgb_fwd_job &jb = jobs[i];
+        const ctgb_params *p = jb.params;
+        if (!p || !jb.table || !jb.vol || !jb.out)
+            return set_error(CTGB_ERR_ARG, "batched forward: job %d has a NULL argument", i);
+        if (jb.view0 < 0 || jb.nviews < 0 || jb.view0 + jb.nviews > p->nviews)
+            return set_error(CTGB_ERR_ARG, "batched forward: job %d view range outside the scan", i);
+        if (jb.epilogue < CTGB_FWD_STORE || jb.epilogue > CTGB_FWD_EM_RATIO)
+            return set_error(CTGB_ERR_ARG, "batched forward: job %d unknown epilogue %d", i, jb.epilogue);
+        if (jb.epilogue != CTGB_FWD_STORE && (!jb.p0 || (jb.epilogue != CTGB_FWD_EM_RATIO && !jb.a1)))
+            return set_error(CTGB_ERR_ARG, "batched forward: job %d epilogue needs p0 and a1", i);
+        std::vector<int> axes;
+        view_axes(p, jb.view0, jb.nviews, axes);
+        sc[i].tr = fwd_tile_rows(p);
+        sc[i].ntu = (p->nu + kTU - 1) / kTU;
+        sc[i].ntiles = sc[i].ntu * ((p->nv + sc[i].tr - 1) / sc[i].tr);
+        for (int v = 0; v < jb.nviews; ++v) {
+            if (axes[v] == 2)
+                return set_error(CTGB_ERR_ARG, "batched forward: job %d view %d is z-dominant (not batched)", i,
+                                 jb.view0 + v);
+            sc[i].views[axes[v]].push_back(v);
+        }
+    }
+    FwdPlanHead head;
+    std::memset(&head, 0, sizeof head);
+    head.magic = kFwdPlanMagic;
+    size_t off = align_up(sizeof head, 128);
+    const int trs[2] = {32, 16};
+    for (int a = 0; a < 2; ++a)
+        for (int t = 0; t < 2; ++t) {
+            FwdPlanGroup g;
+            std::memset(&g, 0, sizeof g);
+            g.xd = a == 0;
+            g.tr = trs[t];
+            long long items = 0, nviews = 0;
+            for (int i = 0; i < njobs; ++i)
+                if (sc[i].tr == g.tr && !sc[i].views[a].empty()) {
+                    ++g.njobs;
+                    items += (long long)sc[i].views[a].size() * sc[i].ntiles;
+                    nviews += (long long)sc[i].views[a].size();
+                }
+            if (!g.njobs) continue;
+            if (items > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "batched forward: too many tiles");
+            g.nitems = (int32_t)items;
+            g.off_jobs = (int64_t)off;
+            off = align_up(off + sizeof(FwdJob) * g.njobs, 128);
+            g.off_views = (int64_t)off;
+            off = align_up(off + sizeof(int32_t) * nviews, 128);
+            head.g[head.ngroups++] = g;
+        }
+    long long titems = 0;
+    for (int i = 0; i < njobs; ++i)
+        if (jobs[i].vol_xzy && !sc[i].views[0].empty()) {
+            const ctgb_params *p = jobs[i].params;
+            ++head.ntrans;
+            titems += (long long)((p->nx + 31) / 32) * ((p->ny + 31) / 32) * p->nz;
+        }
+    if (titems > 0x7fffffffLL) return set_error(CTGB_ERR_SIZE, "batched forward: too many transpose tiles");
+    head.trans_items = (int32_t)titems;
+    head.off_trans = (int64_t)off;
+    off = align_up(off + sizeof(TransJob) * head.ntrans, 128);
+    head.total = (int64_t)off;
+    *need = off;
+    if (!out) return CTGB_OK;
+    if (bytes < off) return set_error(CTGB_ERR_SIZE, "batched forward: plan buffer of %zu bytes below %zu", bytes, off);
+    std::memset(out, 0, off);
+    std::memcpy(out, &head, sizeof head);
+    for (int gi = 0; gi < head.ngroups; ++gi) {
+        const FwdPlanGroup &g = head.g[gi];
+        const int a = g.xd ? 0 : 1;
+        FwdJob *dj = reinterpret_cast<FwdJob *>(out + g.off_jobs);
+        int32_t *dv = reinterpret_cast<int32_t *>(out + g.off_views);
+        int k = 0, item = 0, list = 0;
+        for (int i = 0; i < njobs; ++i) {
+            if (sc[i].tr != g.tr || sc[i].views[a].empty()) continue;
+            const ctgb_fwd_job &jb = jobs[i];
+            const ctgb_params *p = jb.params;
+            FwdJob &f = dj[k++];
+            const uint32_t box[3] = {kBoxX, 1, kBoxZ};
+            bool tma;
+            if (g.xd) {
+                const uint64_t d[3] = {(uint64_t)p->ny, (uint64_t)p->nx, (uint64_t)p->nz};
+                tma = jb.vol_xzy && p->ny % 4 == 0 && ctgb_make_tmap_3d(&f.tm, jb.vol_xzy, d, box);
+                f.src = jb.vol_xzy ? jb.vol_xzy : jb.vol;
+                f.st_k = jb.vol_xzy ? 1LL : (long long)p->nx;
+            } else {
+                const uint64_t d[3] = {(uint64_t)p->nx, (uint64_t)p->ny, (uint64_t)p->nz};
+                tma = p->nx % 4 == 0 && ctgb_make_tmap_3d(&f.tm, jb.vol, d, box);
+                f.src = jb.vol;
+                f.st_k = 1LL;
+            }
+            if (!tma) std::memset(&f.tm, 0, sizeof f.tm);
+            f.T = static_cast<const float *>(jb.table);
+            f.proj = jb.out;
+            f.view0 = jb.view0;
+            f.ntu = sc[i].ntu;
+            f.ntiles = sc[i].ntiles;
+            f.tma = tma ? 1 : 0;
+            f.item0 = item;
+            f.nitems = (int)sc[i].views[a].size() * sc[i].ntiles;
+            f.list0 = list;
+            f.epi.mode = jb.epilogue;
+            f.epi.eps = jb.eps;
+            f.epi.p0 = jb.p0;
+            f.epi.a1 = jb.a1;
+            for (int v : sc[i].views[a]) dv[list++] = v;
+            item += f.nitems;
+        }
+    }
+    TransJob *tj = reinterpret_cast<TransJob *>(out + head.off_trans);
+    int k = 0, item = 0;
+    for (int i = 0; i < njobs; ++i)
+        if (jobs[i].vol_xzy && !sc[i].views[0].empty()) {
+            const ctgb_params *p = jobs[i].params;
+            TransJob &t = tj[k++];
+            t.in = jobs[i].vol;
+            t.out = jobs[i].vol_xzy;
+            t.nx = p->nx; t.ny = p->ny; t.nz = p->nz;
+            t.tx = (p->nx + 31) / 32; t.ty = (p->ny + 31) / 32;
+            t.item0 = item;
+            item += t.tx * t.ty * t.nz;
+        }
+    return CTGB_OK;
+}
+
+template <bool XD, int TR>
+cudaError_t launch_fwd_batch(const FwdPlanGroup &g, const unsigned char *d_plan, int grid, cudaStream_t st,
+                             int *status) {
+    static std::atomic<unsigned long long> attr;
+    cudaError_t e = smem_limit_once((const void *)dd_forward_batch_kernel<XD, TR>, (int)sizeof(FwdTmaSmem<TR>), attr);
+    if (e != cudaSuccess) return e;
+    dd_forward_batch_kernel<XD, TR><<<grid, 32, sizeof(FwdTmaSmem<TR>), st>>>(
+        reinterpret_cast<const FwdJob *>(d_plan + g.off_jobs), g.njobs,
+        reinterpret_cast<const int *>(d_plan + g.off_views), g.nitems, status);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" int ctgb_batch_forward_plan_bytes(const ctgb_fwd_job *jobs, int32_t njobs, size_t *bytes) {
+    clear_error();
+    if (!bytes) return set_error(CTGB_ERR_ARG, "ctgb_batch_forward_plan_bytes: NULL argument");
+    return build_fwd_plan(jobs, njobs, nullptr, 0, bytes);
+}
+
+extern "C" int ctgb_batch_forward_plan(const ctgb_fwd_job *jobs, int32_t njobs, void *host_plan, size_t bytes) {
+    clear_error();
+    if (!host_plan) return set_error(CTGB_ERR_ARG, "ctgb_batch_forward_plan: NULL plan");
+    size_t need = 0;
+    return build_fwd_plan(jobs, njobs, static_cast<unsigned char *>(host_plan), bytes, &need);
+}
+
+extern "C" int ctgb_batch_forward(const void *host_plan, const void *d_plan, int32_t ctas_per_sm, void *stream) {
+    clear_error();
+    if (!host_plan || !d_plan || ctas_per_sm < 1)
+        return set_error(CTGB_ERR_ARG, "ctgb_batch_forward: bad arguments");
+    const FwdPlanHead &head = *static_cast<const FwdPlanHead *>(host_plan);
+    if (head.magic != kFwdPlanMagic) return set_error(CTGB_ERR_ARG, "ctgb_batch_forward: not a forward plan");
+    if (reinterpret_cast<uintptr_t>(d_plan) % 128)
+        return set_error(CTGB_ERR_ARG, "ctgb_batch_forward: device plan must be 128-byte aligned");
+    int sms = 0;
+    if (int st = device_sms(&sms)) return st;
+    int *status = ctgb_status_ptr();
+    if (!status) return set_error(CTGB_ERR_CUDA, "ctgb_batch_forward: device status word unavailable");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned char *dp = static_cast<const unsigned char *>(d_plan);
+    if (head.ntrans > 0) {
+        const int grid = std::min(head.trans_items, sms * 16);
+        transpose_xy_batch_kernel<<<grid, dim3(32, 8), 0, st>>>(reinterpret_cast<const TransJob *>(dp + head.off_trans),
+                                                               head.ntrans, head.trans_items);
+        if (int e = check_launch("transpose_xy_batch_kernel")) return e;
+    }
+    for (int gi = 0; gi < head.ngroups; ++gi) {
+        const FwdPlanGroup &g = head.g[gi];
+        const long long want = (long long)sms * ctas_per_sm;
+        const int grid = (int)std::min<long long>(g.nitems, want);
+        cudaError_t e;
+        if (g.tr == 32) e = g.xd ? launch_fwd_batch<true, 32>(g, dp, grid, st, status)
+                                 : launch_fwd_batch<false, 32>(g, dp, grid, st, status);
+        else e = g.xd ? launch_fwd_batch<true, 16>(g, dp, grid, st, status)
+                      : launch_fwd_batch<false, 16>(g, dp, grid, st, status);
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "dd_forward_batch_kernel: %s", cudaGetErrorString(e));
+    }
+    return CTGB_OK;
 }

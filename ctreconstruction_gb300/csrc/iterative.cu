@@ -15,6 +15,7 @@
 
 #include "../../include/ctgb.h"
 #include "status.h"
+#include "updates.cuh"
 
 namespace ctgb {
 
@@ -31,7 +32,7 @@ static int ew_blocks(long long n) {
 __global__ void sart_residual_kernel(const float *__restrict__ ax, const float *__restrict__ p0,
                                      const float *__restrict__ a1, float eps, float *__restrict__ out, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = (ax[i] - p0[i]) / (a1[i] + eps);
+        out[i] = sart_residual(ax[i], p0[i], a1[i], eps);
 }
 
 // SART.py:55  x = x_prev - alpha * (bp / norm1 + eps)   (eps added after the division, as written)
@@ -39,7 +40,7 @@ __global__ void sart_update_kernel(const float *xp, const float *__restrict__ bp
                                    const float *__restrict__ n1, float alpha, float eps, float *x,
                                    long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        x[i] = xp[i] - alpha * (bp[i] / n1[i] + eps);
+        x[i] = sart_update(xp[i], bp[i], n1[i], alpha, eps);
 }
 
 // EM.py:36-39  p0[Ax == 0] = 0 (in place: the script's proj0 aliases the
@@ -48,9 +49,7 @@ __global__ void em_ratio_kernel(float *__restrict__ p0, const float *__restrict_
                                 float *__restrict__ out, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        float a = ax[i], p = p0[i];
-        if (a == 0.0f) { p = 0.0f; p0[i] = 0.0f; a = eps; }
-        out[i] = p / a;
+        out[i] = em_ratio(p0 + i, ax[i], eps);
     }
 }
 
@@ -58,7 +57,7 @@ __global__ void em_ratio_kernel(float *__restrict__ p0, const float *__restrict_
 __global__ void em_update_kernel(const float *xp, const float *__restrict__ bp,
                                  const float *__restrict__ nrm, float *x, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        x[i] = xp[i] * (bp[i] / nrm[i]);
+        x[i] = em_update(xp[i], bp[i], nrm[i]);
 }
 
 // ASD_POCS.py:174-175  r = (p0 - Ax) / (A1 + eps); r[A1 == 0] = 0
@@ -66,8 +65,7 @@ __global__ void pocs_residual_kernel(const float *__restrict__ p0, const float *
                                      const float *__restrict__ a1, float eps, float *__restrict__ out, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const float d = a1[i];
-        out[i] = (d == 0.0f) ? 0.0f : (p0[i] - ax[i]) / (d + eps);
+        out[i] = pocs_residual(p0[i], ax[i], a1[i], eps);
     }
 }
 
@@ -77,10 +75,7 @@ __global__ void pocs_update_kernel(const float *xp, const float *__restrict__ bp
                                    long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const float d = n1[i];
-        const float b = (d == 0.0f) ? 0.0f : bp[i];
-        const float v = xp[i] + beta * b / (d + eps);
-        x[i] = v < 0.0f ? 0.0f : v;
+        x[i] = pocs_update(xp[i], bp[i], n1[i], beta, eps);
     }
 }
 

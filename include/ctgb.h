@@ -340,6 +340,78 @@ int ctgb_unet_wgrad(const void *x, int32_t cin, const void *g, int32_t cout, flo
  * partials[blocks][c] (the bias gradient after a sum over blocks). */
 int ctgb_unet_colsum(const void *g, int32_t c, int64_t nvox, float *partials, int32_t blocks, void *stream);
 
+/* ---- batched solver launches ------------------------------------------------
+ * The iterative drivers (SART.py, EM.py, ASD_POCS.py and OS-SART, restated in
+ * ctreconstruction_gb300/iterative.py) run one projector after the other per
+ * update; the reference runs one scan at a time with one launch per view
+ * (Reconstruction_numba.py:457-468, :1108-1112).  These entry points run the
+ * forward projections, or the backprojections, of many scans of uneven sizes
+ * in one persistent launch (a fixed grid of CTAs walking a work list of
+ * (scan, view, detector tile) or (scan, voxel-column block) items), and fuse
+ * the drivers' element-wise lines into the projectors' stores: the forward
+ * can store a residual instead of A x, the backprojectors an updated iterate
+ * instead of B r.  No reference counterpart as entry points; the fused lines
+ * are SART.py:51,55, EM.py:36-42 and ASD_POCS.py:174-179.
+ *
+ * A plan is built once on the host (plan_bytes, then plan) from job
+ * descriptions holding device pointers; the caller copies the host plan to a
+ * device buffer of the same size and passes both to the launch function, which
+ * reads launch sizes from the host copy and the jobs from the device copy (no
+ * allocation, no host-to-device copy at launch).  Device plans are 128-byte
+ * aligned.  ctas_per_sm sets the
+ * persistent grid: min(items, SMs * ctas_per_sm) CTAs. */
+#define CTGB_FWD_STORE 0          /* A x                                              */
+#define CTGB_FWD_SART_RESIDUAL 1  /* (A x - p0) / (a1 + eps)                 SART.py:51 */
+#define CTGB_FWD_POCS_RESIDUAL 2  /* (p0 - A x) / (a1 + eps), 0 where a1 == 0         */
+#define CTGB_FWD_EM_RATIO 3       /* p0 / A x; where A x == 0: p0 := 0 in place, 0    */
+#define CTGB_BP_STORE 0           /* vol = (accumulate ? vol : 0) + B r               */
+#define CTGB_BP_SART_UPDATE 1     /* x = x - coef * (B r / n1 + eps)      SART.py:55 */
+#define CTGB_BP_EM_UPDATE 2       /* x = x * (B r / n1)                   EM.py:41-42 */
+#define CTGB_BP_POCS_UPDATE 3     /* x = max(0, x + coef * (n1 == 0 ? 0 : B r) / (n1 + eps)) */
+
+typedef struct {
+    const ctgb_params *params; /* the scan (host)                                         */
+    const void *table;         /* its device geometry table                               */
+    const float *vol;          /* device volume [nz][ny][nx]                              */
+    float *vol_xzy;            /* device [nz][nx][ny] scratch the launch fills (x-dominant views read it); NULL: read vol */
+    float *out;                /* device output of views view0 .. view0 + nviews - 1      */
+    int32_t view0, nviews;
+    int32_t epilogue;          /* CTGB_FWD_*                                              */
+    float eps;
+    float *p0;                 /* measured projections of those views (residual epilogues) */
+    const float *a1;           /* A 1 of those views (SART and POCS residuals)            */
+} ctgb_fwd_job;
+
+int ctgb_batch_forward_plan_bytes(const ctgb_fwd_job *jobs, int32_t njobs, size_t *bytes);
+int ctgb_batch_forward_plan(const ctgb_fwd_job *jobs, int32_t njobs, void *host_plan, size_t bytes);
+/* Transposes (one launch) and forward-projects (one launch per dominant axis
+ * and tile height present) every job of the plan. */
+int ctgb_batch_forward(const void *host_plan, const void *d_plan, int32_t ctas_per_sm, void *stream);
+
+typedef struct {
+    const ctgb_params *params; /* the scan (host)                                         */
+    const void *table;         /* its device geometry table                               */
+    const float *proj;         /* device projections of views view0 .. view0 + nviews - 1 */
+    float *vol;                /* device output volume (CTGB_BP_STORE)                    */
+    void *workspace;           /* device scratch: ctgb_backproject_fdk_workspace_bytes(nviews), all views at once */
+    size_t workspace_bytes;
+    int32_t view0, nviews;
+    float scale;               /* matched: vol = scale * A^T proj; FDK: the dtheta factor */
+    int32_t accumulate;        /* CTGB_BP_STORE only                                      */
+    int32_t epilogue;          /* CTGB_BP_*                                               */
+    float coef, eps;
+    float *x;                  /* iterate updated in place (update epilogues)             */
+    const float *n1;           /* backprojection normaliser (update epilogues)            */
+} ctgb_bp_job;
+
+/* matched != 0: the matched (adjoint) backprojector of ctgb_backproject_matched_ws;
+ * 0: the FDK-weighted one of ctgb_backproject_fdk_ws (all jobs flat, or all curved). */
+int ctgb_batch_backproject_plan_bytes(const ctgb_bp_job *jobs, int32_t njobs, size_t *bytes);
+int ctgb_batch_backproject_plan(const ctgb_bp_job *jobs, int32_t njobs, int32_t matched, void *host_plan,
+                                size_t bytes);
+/* Integrates (one launch) and backprojects (one launch) every job of the plan. */
+int ctgb_batch_backproject(const void *host_plan, const void *d_plan, int32_t ctas_per_sm, void *stream);
+
 /* ---- status ----------------------------------------------------------------
  * ctgb_device_status: the device-side status word of the current device
  * (CTGB_DEVERR_* bits set by kernels whose bounded waits ran out or that

@@ -147,6 +147,35 @@ def test_null_device_pointers_are_rejected_without_a_launch():
                   ctypes.c_void_p(16), 10, 100, 1.0, 0, None)
 
 
+def test_batch_plans_validate_jobs_on_the_host():
+    """The batched plans check their jobs before anything touches a device:
+    no jobs, a view range outside the scan, a missing epilogue operand."""
+    p = ReconstructionParams.from_dict(cone_params(nviews=8)).to_ctgb()
+    n = ctypes.c_size_t(0)
+    fake = ctypes.c_void_p(256)
+    with pytest.raises(ValueError, match="no jobs"):
+        _lib.call("ctgb_batch_forward_plan_bytes", None, 0, ctypes.byref(n))
+    job = _lib.CtgbFwdJob(ctypes.pointer(p), fake, fake, fake, fake, 4, 8, _lib.FWD_STORE, 0.0, None, None)
+    with pytest.raises(ValueError, match="view range"):
+        _lib.call("ctgb_batch_forward_plan_bytes", ctypes.byref(job), 1, ctypes.byref(n))
+    job = _lib.CtgbFwdJob(ctypes.pointer(p), fake, fake, fake, fake, 0, 8, _lib.FWD_POCS_RESIDUAL, 1e-5, None, None)
+    with pytest.raises(ValueError, match="needs p0"):
+        _lib.call("ctgb_batch_forward_plan_bytes", ctypes.byref(job), 1, ctypes.byref(n))
+    job = _lib.CtgbFwdJob(ctypes.pointer(p), fake, fake, fake, fake, 0, 8, _lib.FWD_STORE, 0.0, None, None)
+    _lib.call("ctgb_batch_forward_plan_bytes", ctypes.byref(job), 1, ctypes.byref(n))
+    assert n.value > 0
+    ws = ctypes.c_size_t(0)
+    _lib.call("ctgb_backproject_fdk_workspace_bytes", ctypes.byref(p), 8, ctypes.byref(ws))
+    bj = _lib.CtgbBpJob(ctypes.pointer(p), fake, fake, fake, fake, ws.value - 4, 0, 8, 1.0, 0, _lib.BP_STORE,
+                        0.0, 0.0, None, None)
+    with pytest.raises(ValueError, match="workspace"):
+        _lib.call("ctgb_batch_backproject_plan_bytes", ctypes.byref(bj), 1, ctypes.byref(n))
+    bj = _lib.CtgbBpJob(ctypes.pointer(p), fake, fake, fake, fake, ws.value, 0, 8, 1.0, 0, _lib.BP_EM_UPDATE,
+                        0.0, 0.0, None, None)
+    with pytest.raises(ValueError, match="epilogue output"):
+        _lib.call("ctgb_batch_backproject_plan_bytes", ctypes.byref(bj), 1, ctypes.byref(n))
+
+
 def test_filter_apply_rejects_bad_row_lengths_without_a_launch():
     """ctgb_filter_apply sizes its shared memory from zpl: a length that is not
     a power of two in [2, 8192] is refused on the host (nothing launched)."""
