@@ -12,8 +12,9 @@ part of the product.  Steps:
 2. Compile that file with ``oracle/ref_launch.cpp`` into
    ``oracle/_ref/libctref.so`` with g++ and OpenMP.
 
-The checkout's location comes from the ``ref_root`` argument or the
-``CTGB_REFERENCE_ROOT`` environment variable.  Where neither names a checkout
+The checkout's location comes from the ``ref_root`` argument, else the
+``CTGB_REFERENCE_ROOT`` environment variable, else a checkout named
+``reference`` beside this repository's directory.  Where none names a checkout
 (a machine that only received the working tree), step 1 is skipped and an
 existing ``gfp_kernels.cpp`` is compiled; with neither a checkout nor that
 file, ``build`` raises and says how to point it at the reference.
@@ -32,10 +33,16 @@ OUT = os.path.join(HERE, "_ref")
 ENV_REF = "CTGB_REFERENCE_ROOT"
 
 
+SIBLING_REF = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def reference_root(ref_root=None):
-    """The reference checkout named by the argument or CTGB_REFERENCE_ROOT, or None."""
-    root = ref_root or os.environ.get(ENV_REF)
-    return root if root and os.path.isdir(os.path.join(root, "python")) else None
+    """The reference checkout named by the argument, CTGB_REFERENCE_ROOT or the
+    sibling ``reference`` directory, or None."""
+    for root in (ref_root, os.environ.get(ENV_REF), SIBLING_REF):
+        if root and os.path.isdir(os.path.join(root, "python")):
+            return root
+    return None
 
 
 def extract_kernel_text(ref_root):
@@ -67,7 +74,8 @@ def build(ref_root=None, quiet=True):
     if root:
         src = write_translation_unit(root)
     if not os.path.exists(src):
-        raise RuntimeError("no reference checkout (pass its path or set %s) and no extracted %s"
+        raise RuntimeError("no reference checkout (pass its path, set %s or place it beside the repository "
+                           "as 'reference') and no extracted %s"
                            % (ENV_REF, os.path.relpath(src, os.path.dirname(HERE))))
     lib = os.path.join(OUT, "libctref.so")
     deps = [src, os.path.join(HERE, "ref_launch.cpp"), os.path.join(HERE, "ref_shim.h"), os.path.abspath(__file__)]
