@@ -221,17 +221,15 @@ def run_ours(args):
     bp = torch.empty(P.volume_shape, dtype=torch.float32, device=dev)
     xzy = torch.empty((n, n, n), dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
-    integ = P.integrate(proj)                          # integrated-projection workspace (float2 per cell)
-    names = ("transpose", "forward", "integrate", "backproject_fdk")
+    names = ("transpose", "forward", "backproject_fdk")
     ev = {k: [] for k in names}
-    # backward() = integrate (integrate_rows_kernel) + bp_fdk_integ_kernel:
-    # the same two launches ctgb_backproject_fdk_ws makes, issued one by one
-    # so that each kernel is timed alone.
-    launches_per_step = 1 + P.forward_launches() + 2
+    # backward() = one bp_fdk_walk_kernel launch over all views (the full
+    # orbit's four-fold symmetry; no integrated copy of the projections).
+    launches_per_step = 1 + P.forward_launches() + 1
 
     def step(record=False):
         if record:
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             e[0].record(stream)
         P.transpose(vol, out=xzy)
         if record:
@@ -239,12 +237,9 @@ def run_ours(args):
         P.forward(vol, out=proj, transposed=xzy)
         if record:
             e[2].record(stream)
-        P.integrate(proj, out=integ)
+        P.backproject_fdk(proj, out=bp)
         if record:
             e[3].record(stream)
-        P.backproject_fdk_integrated(integ, out=bp)
-        if record:
-            e[4].record(stream)
             for k, name in enumerate(names):
                 ev[name].append((e[k], e[k + 1]))
 
@@ -272,7 +267,7 @@ def run_ours(args):
     value = ws * vv / (ms / 1e3) / 1e9
 
     kern = {k: sum(a.elapsed_time(b) for a, b in v) / len(v) for k, v in ev.items()}
-    # Dominant kernel: bp_fdk_integ_kernel (one launch over all views) or the
+    # Dominant kernel: bp_fdk_walk_kernel (one launch over all views) or the
     # forward (dd_forward_tma_kernel, one launch per run of same-axis views).
     nfwd = P.forward_launches()
     per_launch = {"forward": kern["forward"] / nfwd, "backproject_fdk": kern["backproject_fdk"]}
@@ -281,7 +276,7 @@ def run_ours(args):
     units = {"forward": vv / nfwd, "backproject_fdk": vv}[dom]      # voxel-views per launch
     alg_bytes = 4.0 * units              # 4 B per voxel-view per direction
     achieved = alg_bytes / (per_launch[dom] / 1e3) / 1e9
-    kname = {"forward": "dd_forward_tma_kernel", "backproject_fdk": "bp_fdk_integ_kernel"}[dom]
+    kname = {"forward": "dd_forward_tma_kernel", "backproject_fdk": "bp_fdk_walk_kernel"}[dom]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(kname),
                 "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": per_launch[dom],
@@ -484,12 +479,10 @@ def run_fdk128(args):
     proj = -torch.log(torch.clamp(counts, min=1.0) / 1e5)
     q = torch.empty_like(proj)
     out = torch.empty(P.volume_shape, device=P.device)
-    integ = P.integrate(proj)
-    # backward() = integrate_rows_kernel + bp_fdk_integ_kernel (the launches
-    # backproject_fdk makes), issued as separate stages so each is timed.
+    # Filtering() then backward() (one bp_fdk_walk_kernel launch: the full
+    # orbit's four-fold symmetry), issued as separate stages so each is timed.
     stages = [("copy", lambda: q.copy_(proj)), ("filter", lambda: P.filter(q)),
-              ("integrate", lambda: P.integrate(q, out=integ)),
-              ("backproject", lambda: P.backproject_fdk_integrated(integ, out=out))]
+              ("backproject", lambda: P.backproject_fdk(q, out=out))]
     ms, per = _timed_stages(stages, args.steps, args.warmup)
     ms -= per["copy"]                      # restoring the input is not part of the step
     vv = 128 ** 3 * 360
@@ -497,7 +490,7 @@ def run_fdk128(args):
     rmse = float(torch.sqrt(torch.mean((out - ph)[inner] ** 2)))
     dom = max(("filter", "backproject"), key=lambda k: per[k])
     if dom == "backproject":
-        roof = hbm_roofline("bp_fdk_integ_kernel", per["backproject"], 4.0 * vv, "4 B per voxel-view")
+        roof = hbm_roofline("bp_fdk_walk_kernel", per["backproject"], 4.0 * vv, "4 B per voxel-view")
     else:
         roof = hbm_roofline("fdk_filter_kernel", per["filter"], 8.0 * 360 * 256 * 192, "8 B per detector pixel")
     roof["per_stage_ms"] = per
@@ -769,8 +762,7 @@ def _asd_roofline_cpu(P, x, args, niter_label="outer iteration"):
     vv = float(n) ** 3 * P.params.NumberOfViews
     nfwd = P.forward_launches()
     cand = {"forward": (per["forward"] / nfwd, 4.0 * vv / nfwd, "dd_forward_tma_kernel", "4 B per voxel-view"),
-            "backproject": (per["backproject"], 4.0 * vv, "bp_fdk_integ_kernel",
-                            "4 B per voxel-view (time includes the integration pass)"),
+            "backproject": (per["backproject"], 4.0 * vv, "bp_fdk_walk_kernel", "4 B per voxel-view"),
             "tv20": (per["tv20"] / 20, 12.0 * n ** 3, "tv_norm_kernel + tv_step_kernel",
                      "12 B per voxel per TV step (read for the norm; read + write for the step)")}
     # dominant: the largest share of one outer iteration (5 forward + 5 backprojections + 1 TV descent)
@@ -965,9 +957,9 @@ def run_rows(args):
     per = detail["dd_pair_curved"]["per_stage_ms"]
     dom = max(per, key=per.get)
     nfwd = Projector(dict(base, DetectorShape='Curved'), device=dev).forward_launches()
-    roof = hbm_roofline({"forward": "dd_forward_tma_kernel", "backproject": "bp_fdk_integ_kernel"}[dom],
+    roof = hbm_roofline({"forward": "dd_forward_tma_kernel", "backproject": "bp_fdk_walk_kernel"}[dom],
                         per[dom] / (nfwd if dom == "forward" else 1), 4.0 * vv / (nfwd if dom == "forward" else 1),
-                        "4 B per voxel-view, curved detector (backprojection time includes its integration pass)")
+                        "4 B per voxel-view, curved detector")
     cpu = None
     if not args.no_cpu:
         # Curved detectors run only in the reference's numba flavour (its

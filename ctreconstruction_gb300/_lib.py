@@ -75,6 +75,8 @@ SIGNATURES = {
     "ctgb_forward_static": [_P, _vp, _vp, _vp, _i32, _i32, _vp],
     "ctgb_transpose_xy": [_vp, _vp, _i32, _i32, _i32, _vp],
     "ctgb_backproject_fdk": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
+    "ctgb_backproject_fdk_orbit_size": [_P, ctypes.POINTER(_i32)],
+    "ctgb_backproject_fdk_orbits": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_backproject_matched": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp],
     "ctgb_backproject_fdk_workspace_bytes": [_P, _i32, ctypes.POINTER(_sz)],
     "ctgb_backproject_fdk_ws": [_P, _vp, _vp, _vp, _i32, _i32, _f32, _i32, _vp, _sz, _vp],

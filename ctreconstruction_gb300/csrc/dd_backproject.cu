@@ -9,12 +9,16 @@
 //    arc detector), the covered detector cells are weighted by overlap fraction
 //    and the sum is scaled by R^2/(R - y_c)^2 and dtheta.
 //
-//    GB300 layout: one thread owns a column of kZc voxels (fixed x, y) and
-//    keeps their sums in registers across all views (no atomics; the reference
-//    launches one kernel per view and atomically adds).  Everything that does
-//    not depend on z — the four rotated xy corners, the u footprint, the
-//    distance weight — is computed once per (column, view); per voxel only the
-//    v footprint (two products and a min/max per z end) is new.  With
+//    GB300 layout: one thread owns a column of voxels (fixed x, y) and keeps
+//    their sums on chip across all views (no atomics; the reference launches
+//    one kernel per view and atomically adds).  Everything that does not
+//    depend on z — the four rotated xy corners, the u footprint, the distance
+//    weight — is computed once per (column, view); per voxel only the v
+//    footprint (two products and a min/max per z end) is new.  Two forms:
+//    bp_fdk_walk_kernel walks the detector rows under the column on the raw
+//    projections (and shares each set-up between the columns of a rotation
+//    orbit on symmetric scans); bp_fdk_integ_kernel looks the rows up in
+//    integrated projections.  With
 //    angle2 = 0 the reference's corner slopes are (S_z - z_c) / (S_y - y_c); the
 //    min/max over the 8 corners equals the min/max over {S_z - z_lo, S_z - z_hi}
 //    x {min, max of 1/(S_y - y_c)}.
@@ -28,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "dd_common.cuh"
@@ -40,20 +45,9 @@ namespace ctgb {
 constexpr int kBpTileX = 32, kBpTileY = 4;
 
 // ---------------------------------------------------------------------------
-// FDK-weighted DD backprojection, table form (the default path).
-//
-// Per (voxel column, view) the u footprint is z-independent, so the column
-// first builds G(m) = sum_l Q[m][l] * w_u(l) for the detector rows its kBpZ
-// voxels can reach, with running sums C(m) = sum_{m' < m} G(m'), in shared
-// memory.  Each voxel's v footprint [lo, hi] (detector-row units) then costs
-// two lookups: integral = (C + G*frac)(hi) - (C + G*frac)(lo), divided by the
-// footprint width — the reference's weight_calculator1 sum written as an
-// integral of a piecewise-constant function.  With the source outside the
+// Helpers of the FDK-weighted backprojectors.  With the source outside the
 // volume every corner depth 1/(S_y - y_c) is positive, so the min/max over the
-// 8 corner slopes reduces to one product per z end.  Columns whose footprint
-// falls outside these assumptions (more than 4 u cells, more than kBpRows rows,
-// a corner behind the source) take the direct per-cell loop.
-constexpr int kBpZ = 16, kBpRows = 24, kBpTX = 32, kBpTY = 4;
+// 8 corner slopes reduces to one product per z end (v_footprint).
 
 __device__ __forceinline__ float fast_rcp(float x) { return __fdividef(1.0f, x); }
 
@@ -70,154 +64,6 @@ __device__ __forceinline__ void v_footprint(float zc, float hz, float Sz, float 
     const float va = fmaf(a, Mv, Av), vb = fmaf(b, Mv, Av);
     *lo = fminf(va, vb);
     *hi = fmaxf(va, vb);
-}
-
-template <bool CURVED>
-__global__ void __launch_bounds__(kBpTX * kBpTY, 6)
-bp_fdk_table_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
-                    int nviews, float scale, int accumulate) {
-    __shared__ float2 gtab[kBpRows][kBpTX * kBpTY];
-    const TableHeader &h = header(T);
-    const int tid = threadIdx.y * kBpTX + threadIdx.x;
-    const int ix = blockIdx.x * kBpTX + threadIdx.x;
-    const int iy = blockIdx.y * kBpTY + threadIdx.y;
-    const int z0 = blockIdx.z * kBpZ;
-    const bool live = ix < h.nx && iy < h.ny;
-    const int ixc = min(ix, h.nx - 1), iyc = min(iy, h.ny - 1);
-    const float *__restrict__ ki = T + h.off_ki;
-    const float *__restrict__ pp = T + h.off_pp;
-    const int nu = h.nu, nv = h.nv, nz = h.nz;
-    const int zlast = min(z0 + kBpZ, nz) - 1 - z0;            // last voxel of the chunk (relative)
-    const float xx = T[h.off_xpix + ixc], yy = T[h.off_ypix + iyc];
-    const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f, dzs = h.dz;
-    const float du = h.du_bp, dv = h.dv_bp, inv_du = 1.0f / du, inv_dv = 1.0f / dv;
-    const float ki0 = ki[0], pp0 = pp[0];
-    const float Sx = h.src0x, Sy = h.src0y, Dy = h.det0y, R = h.sad;
-    const float eps = h.eps_bp;
-    const float zfirst = T[h.off_zpix + min(z0, nz - 1)];
-    float acc[kBpZ];
-#pragma unroll
-    for (int j = 0; j < kBpZ; ++j) acc[j] = 0.0f;
-
-    for (int vi = 0; vi < nviews; ++vi) {
-        const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
-        const float cs = V[VF_COS], sn = V[VF_SIN], Sz = V[VF_BPSZ];
-        const float *__restrict__ Q = proj + (long long)vi * nu * nv;
-        const float yc = yy * cs - xx * sn;
-        float umin = INFINITY, umax = -INFINITY, imin = INFINITY, imax = -INFINITY;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float cx = xx + ((q & 1) ? hx : -hx), cy = yy + ((q & 2) ? hy : -hy);
-            const float xr = cx * cs + cy * sn, yr = cy * cs - cx * sn;
-            const float inv = fast_rcp(Sy - yr);
-            const float su = (Sx - xr) * inv;
-            umin = fminf(umin, su); umax = fmaxf(umax, su);
-            imin = fminf(imin, inv); imax = fmaxf(imax, inv);
-        }
-        float cu1, cu2;
-        if (CURVED) { cu1 = -atanf(umin); cu2 = -atanf(umax); }
-        else { cu1 = fmaf(umin, Dy - Sy, Sx); cu2 = fmaf(umax, Dy - Sy, Sx); }
-        const float ua = (cu1 - ki0) * inv_du, ub = (cu2 - ki0) * inv_du;
-        const float ulo = fminf(ua, ub), uhi = fmaxf(ua, ub);
-        float fl0;
-        const int l0 = floor_split(ulo, &fl0);
-        const float uw = uhi - ulo;
-        const float Rd = R - yc;
-        const float W = scale * (R * R) * fast_rcp(Rd * Rd);
-        const float Mv = (Dy - Sy) * inv_dv, Av = (Sz - pp0) * inv_dv;
-        // Rows the chunk's footprints reach: footprints move monotonically with z,
-        // so the first and last voxels bound them (one row of margin each side).
-        float vlo0, vhi0, vloN, vhiN;
-        v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &vlo0, &vhi0);
-        v_footprint(zfirst + (float)zlast * dzs, hz, Sz, imin, imax, Mv, Av, &vloN, &vhiN);
-        const int mlo = (int)floorf(fminf(vlo0, vloN)) - 1;
-        const int mhi = (int)floorf(fmaxf(vhi0, vhiN)) + 1;
-        const bool simple = live && imin > 0.0f && (uhi - fl0) <= 4.0f && (mhi - mlo + 1 <= kBpRows);
-        if (simple) {
-            float ov[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t)
-                ov[t] = fmaxf(0.0f, fminf(fl0 + (float)(t + 1), uhi) - fmaxf(fl0 + (float)t, ulo));
-            float wscale = W;
-            if (uw > 1e-6f) wscale *= fast_rcp(uw);
-            else { ov[0] = 1.0f; ov[1] = ov[2] = ov[3] = 0.0f; }
-            int ntl = 1;
-#pragma unroll
-            for (int t = 1; t < 4; ++t) ntl = (ov[t] > 0.0f) ? t + 1 : ntl;
-            // G(m) with running sums C(m) for rows mlo..mhi.
-            const bool inner = l0 >= 0 && l0 + 3 < nu;
-            float run = 0.0f;
-            const int nrows = mhi - mlo + 1;
-            for (int i = 0; i < nrows; ++i) {
-                const int m = mlo + i;
-                float g = 0.0f;
-                if (m >= 0 && m < nv) {
-                    const float *__restrict__ row = Q + (long long)m * nu + l0;
-                    if (inner) {
-                        g = __ldg(row) * ov[0] + __ldg(row + 1) * ov[1];
-                        if (ntl > 2) g += __ldg(row + 2) * ov[2];
-                        if (ntl > 3) g += __ldg(row + 3) * ov[3];
-                    } else {
-#pragma unroll
-                        for (int t = 0; t < 4; ++t)
-                            if (t < ntl && l0 + t >= 0 && l0 + t < nu) g += __ldg(row + t) * ov[t];
-                    }
-                }
-                gtab[i][tid] = make_float2(run, g);
-                run += g;
-            }
-#pragma unroll
-            for (int j = 0; j < kBpZ; ++j) {
-                float vlo, vhi, fa, fb;
-                v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &vlo, &vhi);
-                const int ma = min(max(floor_split(vlo, &fa) - mlo, 0), kBpRows - 1);
-                const int mb = min(max(floor_split(vhi, &fb) - mlo, 0), kBpRows - 1);
-                const float2 A = gtab[ma][tid];
-                const float2 B = gtab[mb][tid];
-                const float width = vhi - vlo;
-                const float integ = (B.x + B.y * (vhi - fb)) - (A.x + A.y * (vlo - fa));
-                const float val = (width > 1e-6f) ? integ * fast_rcp(width) : A.y;
-                acc[j] = fmaf(val, wscale, acc[j]);
-            }
-        } else if (live) {
-            // Direct per-cell loop (reference weight calculators).
-            const Span us = make_span(cu1, cu2, ki0, inv_du);
-            const int c0 = max(us.s, 0), c1 = min(us.e, nu - 1);
-            const float abs_du = fabsf(du), abs_dv = fabsf(dv);
-            for (int j = 0; j <= zlast; ++j) {
-                const float zc = zfirst + (float)j * dzs;
-                const float nlo = Sz - (zc - hz), nhi = Sz - (zc + hz);
-                const float a0 = nlo * imin, a1 = nlo * imax, a2 = nhi * imin, a3 = nhi * imax;
-                const float vmn = fminf(fminf(a0, a1), fminf(a2, a3));
-                const float vmx = fmaxf(fmaxf(a0, a1), fmaxf(a2, a3));
-                const float cv1 = fmaf(vmn, Dy - Sy, Sz), cv2 = fmaf(vmx, Dy - Sy, Sz);
-                const Span vs = make_span(cv1, cv2, pp0, inv_dv);
-                const int k0 = max(vs.s, 0), k1 = min(vs.e, nv - 1);
-                float sum = 0.0f;
-                for (int k = k0; k <= k1; ++k) {
-                    const float w1 = span_weight<true>(vs, k, pp[k], pp[k + 1], abs_dv, eps);
-                    const float *__restrict__ qrow = Q + (long long)k * nu;
-                    float part = 0.0f;
-                    for (int l = c0; l <= c1; ++l)
-                        part += __ldg(qrow + l) * span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
-                    sum += part * w1;
-                }
-                gtab[j][tid] = make_float2(sum * W, 0.0f);
-            }
-#pragma unroll
-            for (int j = 0; j < kBpZ; ++j)
-                if (j <= zlast) acc[j] += gtab[j][tid].x;
-        }
-    }
-    if (!live) return;
-#pragma unroll
-    for (int j = 0; j < kBpZ; ++j) {
-        const int iz = z0 + j;
-        if (iz < nz) {
-            float *dst = vol + ((long long)iz * h.ny + iy) * h.nx + ix;
-            *dst = accumulate ? *dst + acc[j] : acc[j];
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -576,6 +422,340 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
     const ParamSrc src = {T, integ, nullptr, nullptr, view0, nviews, scale};
     bp_fdk_column<CURVED>(src, blockIdx.x, blockIdx.y, blockIdx.z,
                           [=](long long i, float b) { vol[i] = accumulate ? __fadd_rn(vol[i], b) : b; });
+}
+
+// ---------------------------------------------------------------------------
+// FDK-weighted DD backprojection by a row walk over the raw projections.
+//
+// Per (voxel column, view) the u footprint's taps (columns lbase + t, overlap
+// weights w_t with the distance weight folded in) hold for every voxel of the
+// column, so detector row r contributes one value R(r) = sum_t w_t p[r][lbase
+// + t].  The column's voxel footprints [lo, hi] (row units) move
+// monotonically with z and consecutive ones overlap by less than a row, so
+// the thread walks up the rows once per (column, view), keeping
+// G(r) = sum_{r' < r} R(r') and the R of the rows at the walk front in
+// registers: a voxel's footprint integral is G(hi) - G(lo) with
+// G(v) = G(floor v) + R(floor v) frac(v), divided by the footprint's width —
+// the reference's weight_calculator1 sum over rows.  Each detector row under
+// the column is read once per view (NT 4-byte loads) instead of two 8-byte
+// running-sum lookups per tap and voxel, and no integrated copy of the
+// projections is made.
+//
+// Four-fold symmetry (NC = 4).  On a full circular orbit whose view count is
+// a multiple of 4, with a square grid centred on the rotation axis, the
+// column (x, y) at angle theta and the column (-y, x) at theta + pi/2 have the
+// same rotated corners, hence the same taps and voxel footprints.  A thread
+// then owns the four columns of one rotation orbit (indices (i, j), (j, n-1-i),
+// (n-1-i, n-1-j), (n-1-j, i)): every (column, view) set-up and every voxel's
+// footprint is computed once and serves four column-views, whose rows are
+// walked side by side.
+constexpr int kWkTX = 4, kWkTY = 32, kWkThreads = kWkTX * kWkTY;   // 4 x 32 columns per CTA, 4 x 8 per warp
+// Z voxels per column chunk and resident CTAs per SM.  The voxel sums live in
+// shared memory (Z * NC floats per thread, each thread its own slots), so the
+// voxel loop stays rolled: with the sums in registers and the loop unrolled,
+// the code outgrew the instruction cache (stalls on instruction fetch were
+// the largest stall reason) and 96 registers still spilled.
+template <int NC> struct WalkShape;
+template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8; };
+template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8; };
+// Quarter-turn orbits: at 512^3 / 720 views Z = 12 with 7 CTAs per SM took
+// 140.3 ms (Z = 8 at 8 CTAs 152.2, Z = 16 at 6 CTAs 146.8, Z = 24 at 4
+// 146.7, Z = 32 at 3 181.0; the voxel loop unrolled by 2 or 4: 157, 159 at
+// Z = 16): a longer chunk shares each (column, view) set-up between more
+// voxels, fewer resident warps hide less of the row loads' latency.
+#ifndef CTGB_WALK_Z4
+#define CTGB_WALK_Z4 12
+#endif
+#ifndef CTGB_WALK_B4
+#define CTGB_WALK_B4 7
+#endif
+template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = CTGB_WALK_B4; };
+
+// Walk rows upwards through one chunk of Z voxels for NC column-views.
+// vb[k]: view k's projections at column lbase, row 0.  Voxel j's footprint
+// comes from the linear model (lin) or from v_footprint.  CLAMP: rows outside
+// [0, nv) read as zero.  The caller has checked that the footprints' rows
+// grow with j, that footprints are at most 2.5 rows wide, advance at most 2.5
+// rows per voxel and overlap their predecessor by under one row, so three row
+// steps per voxel always suffice.  (With the source at +y and the detector
+// at -y, as in every reference script, rows grow with the voxel index: row
+// coordinates run opposite to z on both axes.)  Voxel j of view k adds into
+// sacc[(j * NC + k) * kWkThreads].
+#ifndef CTGB_WALK_UNROLL
+#define CTGB_WALK_UNROLL 1
+#endif
+constexpr int kWalkUnroll = CTGB_WALK_UNROLL;
+template <int NC, int Z, int NT, bool CLAMP>
+__device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, int nv, const float (&ov)[4],
+                                          bool lin, float lo0, float hi0, float dlo, float dhi,
+                                          float zfirst, float dzs, float hz, float Sz, float imin, float imax,
+                                          float Mv, float Av, float *sacc) {
+    auto pos = [&](int j) {
+        if (lin) return __ffma2_rn(make_float2((float)j, (float)j), make_float2(dlo, dhi), make_float2(lo0, hi0));
+        float a, b;
+        v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &a, &b);
+        return make_float2(a, b);
+    };
+    // R of row r for each view; rows outside the detector read row 0 and count zero
+    auto rows = [&](int r, int roff, float (&out)[NC]) {
+        const bool in = !CLAMP || (unsigned)r < (unsigned)nv;
+        const int off = in ? roff : 0;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            const float *__restrict__ q = vb[k] + off;
+            float t0 = 0.0f;
+#pragma unroll
+            for (int t = 0; t < NT; ++t) t0 = fmaf(ov[t], __ldg(q + t), t0);
+            out[k] = in ? t0 : 0.0f;
+        }
+    };
+    const float2 p0 = pos(0);
+    float curf;
+    int cur = floor_split(p0.x, &curf);
+    int roff = cur * nu;
+    float Gc[NC], Rc[NC], Rp[NC], Rn[NC];   // G(cur), R(cur), R(cur - 1), R(cur + 1)
+    rows(cur, roff, Rc);
+    rows(cur + 1, roff + nu, Rn);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) { Gc[k] = 0.0f; Rp[k] = 0.0f; }
+    auto advance = [&]() {
+        cur += 1;
+        roff += nu;
+        curf += 1.0f;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+            Gc[k] += Rc[k];
+            Rp[k] = Rc[k];
+            Rc[k] = Rn[k];
+        }
+        rows(cur + 1, roff + nu, Rn);
+    };
+#pragma unroll (kWalkUnroll)
+    for (int j = 0; j < Z; ++j) {
+        const float2 p = pos(j);
+        const float rw = fast_rcp(p.y - p.x);
+        // lo lies in row cur or cur - 1; G(lo) = G(cur) + R(row) (lo - cur) either way
+        const float dl = p.x - curf;
+        float glo[NC];
+#pragma unroll
+        for (int k = 0; k < NC; ++k) glo[k] = fmaf(dl >= 0.0f ? Rc[k] : Rp[k], dl, Gc[k]);
+#pragma unroll 1
+        for (int a = 0; a < 3 && p.y - curf >= 1.0f; ++a) advance();
+        const float dh = p.y - curf;
+        float *__restrict__ sa = sacc + j * NC * kWkThreads;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) sa[k * kWkThreads] += (fmaf(Rc[k], dh, Gc[k]) - glo[k]) * rw;
+    }
+}
+
+// NC = 1: views [view0, view0 + nviews) of the scan, proj holding them.
+// NC = 2 or 4: base views w in [view0, view0 + nviews) within the first 1/NC
+// of the orbit; each w takes set-up views w + d Q (d < NC, Q = views / NC) and
+// column k of the orbit reads view (w + (d + k) Q) mod views; proj holds
+// every view of the scan.  The grid covers the columns (NC = 1), the lower
+// half of the rows (NC = 2) or one quadrant (NC = 4).
+template <bool CURVED, int NC>
+__global__ void __launch_bounds__(kWkThreads, WalkShape<NC>::MINB)
+bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
+                   int nviews, float scale, int accumulate) {
+    constexpr int Z = WalkShape<NC>::Z;
+    __shared__ float sacc_all[Z * NC * kWkThreads];
+    const int tid = threadIdx.y * kWkTX + threadIdx.x;
+    float *sacc = sacc_all + tid;
+#pragma unroll 1
+    for (int i = 0; i < Z * NC; ++i) sacc[i * kWkThreads] = 0.0f;
+    const TableHeader &h = header(T);
+    const int nu = h.nu, nv = h.nv, nz = h.nz, nxh = h.nx, nyh = h.ny;
+    const int ix = blockIdx.x * kWkTX + threadIdx.x;
+    const int iy = blockIdx.y * kWkTY + threadIdx.y;
+    const bool live = NC == 1 ? (ix < nxh && iy < nyh)
+                    : NC == 2 ? (ix < nxh && iy < nyh / 2) : (ix < nxh / 2 && iy < nxh / 2);
+    const int ixc = min(ix, nxh - 1), iyc = min(iy, nyh - 1);
+    const int z0 = blockIdx.z * Z;
+    const float *__restrict__ ki = T + h.off_ki;
+    const float *__restrict__ pp = T + h.off_pp;
+    const float xx = T[h.off_xpix + ixc], yy = T[h.off_ypix + iyc];
+    const float hx = h.dx * 0.5f, hy = h.dy * 0.5f, hz = h.dz * 0.5f, dzs = h.dz;
+    const float du = h.du_bp, dv = h.dv_bp, inv_du = 1.0f / du, inv_dv = 1.0f / dv;
+    const float ki0 = ki[0], pp0 = pp[0];
+    const float Sx = h.src0x, Sy = h.src0y, Dy = h.det0y, R = h.sad;
+    const float eps = h.eps_bp;
+    const float zfirst = T[h.off_zpix + min(z0, nz - 1)];
+    const int zlast = min(z0 + Z, nz) - 1 - z0;
+    const float inv_zlast = zlast > 0 ? 1.0f / (float)zlast : 0.0f;
+    const int nall = h.nviews, Q = nall / NC;   // views per 1/NC turn
+    const long long vstride = (long long)nu * nv;
+    const float Mv = (Dy - Sy) * inv_dv;
+    const float smax_base = fabsf(dzs * Mv);
+
+    const int nsetup = NC * nviews;
+#pragma unroll 1
+    for (int it = 0; it < nsetup; ++it) {
+        int sview;
+        int pv[NC];
+        if (NC == 1) {
+            sview = view0 + it;
+            pv[0] = it;
+        } else {
+            sview = view0 + it / NC + (it % NC) * Q;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+                const int v = sview + k * Q;
+                pv[k] = v < nall ? v : v - nall;
+            }
+        }
+        const float *__restrict__ V = T + h.off_views + (long long)sview * h.view_stride;
+        const float cs = V[VF_COS], sn = V[VF_SIN], Sz = V[VF_BPSZ];
+        const float yc = yy * cs - xx * sn;
+        float umin = INFINITY, umax = -INFINITY, imin = INFINITY, imax = -INFINITY;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float cxq = xx + ((q & 1) ? hx : -hx), cyq = yy + ((q & 2) ? hy : -hy);
+            const float xr = cxq * cs + cyq * sn, yr = cyq * cs - cxq * sn;
+            const float inv = fast_rcp(Sy - yr);
+            const float su = (Sx - xr) * inv;
+            umin = fminf(umin, su); umax = fmaxf(umax, su);
+            imin = fminf(imin, inv); imax = fmaxf(imax, inv);
+        }
+        float cu1, cu2;
+        if (CURVED) { cu1 = -atanf(umin); cu2 = -atanf(umax); }
+        else { cu1 = fmaf(umin, Dy - Sy, Sx); cu2 = fmaf(umax, Dy - Sy, Sx); }
+        const float ua = (cu1 - ki0) * inv_du, ub = (cu2 - ki0) * inv_du;
+        const float ulo = fminf(ua, ub), uhi = fmaxf(ua, ub);
+        float fl0;
+        const int l0 = floor_split(ulo, &fl0);
+        const float uw = uhi - ulo;
+        const float Rd = R - yc;
+        float wscale = scale * (R * R) * fast_rcp(Rd * Rd);
+        float ovr[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int l = l0 + t;
+            const float o = fmaxf(0.0f, fminf(fl0 + (float)(t + 1), uhi) - fmaxf(fl0 + (float)t, ulo));
+            ovr[t] = (l >= 0 && l < nu) ? o : 0.0f;   // cells off the detector add nothing
+        }
+        if (uw > 1e-6f) wscale *= fast_rcp(uw);
+        else { ovr[0] = (l0 >= 0 && l0 < nu) ? 1.0f : 0.0f; ovr[1] = ovr[2] = ovr[3] = 0.0f; }
+        const bool inner = l0 >= 0 && l0 + 4 <= nu;
+        const int lbase = inner ? l0 : min(max(l0, 0), max(nu - 4, 0));
+        float ov[4];
+        if (__all_sync(0xffffffffu, inner)) {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) ov[t] = ovr[t] * wscale;
+        } else {
+            const int shift = lbase - l0;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int src = t + shift;
+                float w = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) w = (src == k) ? ovr[k] : w;
+                ov[t] = w * wscale;
+            }
+        }
+        int ntl = 1;
+#pragma unroll
+        for (int t = 1; t < 4; ++t) ntl = (ov[t] != 0.0f) ? t + 1 : ntl;
+        const float Av = (Sz - pp0) * inv_dv;
+        const float zend = zfirst + (float)zlast * dzs;
+        const float ztop = fmaxf(zfirst, zfirst + (float)(Z - 1) * dzs) + fabsf(hz);
+        const float zbot = fminf(zfirst, zfirst + (float)(Z - 1) * dzs) - fabsf(hz);
+        const bool linear = (Sz - ztop > 0.0f) || (Sz - zbot < 0.0f);
+        float lo0, hi0, loN, hiN;
+        v_footprint(zfirst, hz, Sz, imin, imax, Mv, Av, &lo0, &hi0);
+        v_footprint(zend, hz, Sz, imin, imax, Mv, Av, &loN, &hiN);
+        const float dlo = (loN - lo0) * inv_zlast, dhi = (hiN - hi0) * inv_zlast;
+        // Footprints of the first two and last two voxels: linear model, or
+        // exact where the chunk straddles the source height.
+        auto posx = [&](int j) {
+            if (linear) return make_float2(fmaf((float)j, dlo, lo0), fmaf((float)j, dhi, hi0));
+            float a, b;
+            v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &a, &b);
+            return make_float2(a, b);
+        };
+        const float2 fa = posx(0), fb = posx(1), fc = posx(Z - 2), fd = posx(Z - 1);
+        const float wa = fa.y - fa.x, wd = fd.y - fd.x;
+        const bool ok = live && imin > 0.0f && (uhi - fl0) <= 4.0f && nu >= 4 &&
+                        smax_base * imax <= 2.5f && wa >= 1e-4f && wa <= 2.5f && wd >= 1e-4f && wd <= 2.5f &&
+                        fa.y - fb.x < 0.999f && fc.y - fd.x < 0.999f && fb.y >= fa.y && fd.y >= fc.y &&
+                        fa.x > -1e6f && fd.y < 1e6f;
+        const int nt = __reduce_max_sync(0xffffffffu, ok ? ntl : 1);
+        const bool inside = fa.x >= 0.0f && fd.y < (float)(nv - 1);
+        const bool clamp = !__all_sync(0xffffffffu, inside || !ok);
+        const bool lin = __all_sync(0xffffffffu, linear || !ok);
+        if (ok) {
+            const float *vb[NC];
+#pragma unroll
+            for (int k = 0; k < NC; ++k) vb[k] = proj + (long long)pv[k] * vstride + lbase;
+#define CTGB_WALK(NTV, C) \
+    walk_rows<NC, Z, NTV, C>(vb, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, sacc)
+            if (!clamp) {
+                if (nt <= 2) CTGB_WALK(2, false);
+                else if (nt == 3) CTGB_WALK(3, false);
+                else CTGB_WALK(4, false);
+            } else {
+                if (nt <= 2) CTGB_WALK(2, true);
+                else if (nt == 3) CTGB_WALK(3, true);
+                else CTGB_WALK(4, true);
+            }
+#undef CTGB_WALK
+        } else if (live) {
+            // Reference weight calculators on the raw values.
+            const Span us = make_span(cu1, cu2, ki0, inv_du);
+            const int c0 = max(us.s, 0), c1 = min(us.e, nu - 1);
+            const float abs_du = fabsf(du), abs_dv = fabsf(dv);
+            const float Wd = scale * (R * R) / (Rd * Rd);
+#pragma unroll 1
+            for (int j = 0; j <= zlast; ++j) {
+                const float zc = zfirst + (float)j * dzs;
+                const float nlo = Sz - (zc - hz), nhi = Sz - (zc + hz);
+                const float a0 = nlo * imin, a1 = nlo * imax, a2 = nhi * imin, a3 = nhi * imax;
+                const float vmn = fminf(fminf(a0, a1), fminf(a2, a3));
+                const float vmx = fmaxf(fmaxf(a0, a1), fmaxf(a2, a3));
+                const float cv1 = fmaf(vmn, Dy - Sy, Sz), cv2 = fmaf(vmx, Dy - Sy, Sz);
+                const Span vs = make_span(cv1, cv2, pp0, inv_dv);
+                const int k0 = max(vs.s, 0), k1 = min(vs.e, nv - 1);
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                    const float *__restrict__ Qv = proj + (long long)pv[k] * vstride;
+                    float sum = 0.0f;
+                    for (int r = k0; r <= k1; ++r) {
+                        const float w1 = span_weight<true>(vs, r, pp[r], pp[r + 1], abs_dv, eps);
+                        const float *__restrict__ qrow = Qv + (long long)r * nu;
+                        float part = 0.0f;
+                        for (int l = c0; l <= c1; ++l)
+                            part += __ldg(qrow + l) * span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
+                        sum += part * w1;
+                    }
+                    sacc[(j * NC + k) * kWkThreads] += sum * Wd;
+                }
+            }
+        }
+    }
+    if (!live) return;
+    const int n1 = nxh - 1;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+        // column k of the orbit: (i, j), (j, n-1-i), (n-1-i, n-1-j), (n-1-j, i)
+        // for quarter turns, (i, j), (nx-1-i, ny-1-j) for half turns
+        int cx, cy;
+        if (NC == 2) {
+            cx = k == 0 ? ix : n1 - ix;
+            cy = k == 0 ? iy : nyh - 1 - iy;
+        } else {
+            cx = k == 0 ? ix : k == 1 ? iy : k == 2 ? n1 - ix : n1 - iy;
+            cy = k == 0 ? iy : k == 1 ? n1 - ix : k == 2 ? n1 - iy : ix;
+        }
+#pragma unroll 1
+        for (int j = 0; j < Z; ++j) {
+            const int iz = z0 + j;
+            if (iz < nz) {
+                float *dst = vol + ((long long)iz * nyh + cy) * nxh + cx;
+                const float b = sacc[(j * NC + k) * kWkThreads];
+                *dst = accumulate ? __fadd_rn(*dst, b) : b;
+            }
+        }
+    }
 }
 
 // ---- matched (adjoint) backprojector ---------------------------------------
@@ -1141,6 +1321,112 @@ static int launch_bp_integ(const ctgb_params *p, const float *T, const float2 *w
     return CTGB_OK;
 }
 
+// Largest rotation-orbit size the FDK walk uses (1, 2 or 4).
+#ifndef CTGB_WALK_NC
+#define CTGB_WALK_NC 4
+#endif
+
+// Half-turn symmetry of a scan for bp_fdk_walk_kernel<.., 2, ..>: a grid of
+// even height centred on the rotation axis (voxel centres i and n-1-i exact
+// negatives of each other in x and in y), no helical pitch, and an even view
+// count whose float32 cosines and sines change sign every half of the views.
+static bool fdk_twofold(const ctgb_params *p) {
+    if ((p->ny & 1) || p->ny < 2) return false;
+    if (p->recon_center[0] != 0.0 || p->recon_center[1] != 0.0 || p->pitch != 0.0) return false;
+    const int n = p->nviews, q = n / 2;
+    if (n < 2 || n % 2) return false;
+    const double step = (p->end_angle - p->start_angle) / n;
+    for (int v = 0; v < n; ++v) {
+        const double a = v * step + p->start_angle, b = ((v + q) % n) * step + p->start_angle;
+        const float ca = (float)std::cos(a), sa = (float)std::sin(a), cb = (float)std::cos(b), sb = (float)std::sin(b);
+        if (std::fabs(cb + ca) > 2.4e-7f || std::fabs(sb + sa) > 2.4e-7f) return false;
+    }
+    return true;
+}
+
+// Four-fold symmetry of a scan for bp_fdk_walk_kernel<.., 4, ..>: a square
+// grid of even side centred on the rotation axis (x and y voxel centres exact
+// negatives of each other in the table), no helical pitch, and a view count
+// divisible by 4 whose float32 cosines and sines repeat, rotated by a quarter
+// turn, every quarter of the views (a full circular orbit).
+static bool fdk_fourfold(const ctgb_params *p) {
+    if (p->nx != p->ny || (p->nx & 1) || p->nx < 2 || p->dx != p->dy) return false;
+    if (p->recon_center[0] != 0.0 || p->recon_center[1] != 0.0 || p->pitch != 0.0) return false;
+    const int n = p->nviews, q = n / 4;
+    if (n < 4 || n % 4) return false;
+    const double step = (p->end_angle - p->start_angle) / n;
+    for (int v = 0; v < n; ++v) {
+        const double a = v * step + p->start_angle, b = ((v + q) % n) * step + p->start_angle;
+        const float ca = (float)std::cos(a), sa = (float)std::sin(a), cb = (float)std::cos(b), sb = (float)std::sin(b);
+        if (std::fabs(cb + sa) > 2.4e-7f || std::fabs(sb - ca) > 2.4e-7f) return false;
+    }
+    return true;
+}
+
+template <int NC>
+static void launch_walk(bool curved, dim3 grid, cudaStream_t s, const float *T, const float *proj, float *vol,
+                        int view0, int nviews, float scale, int accumulate) {
+    dim3 block(kWkTX, kWkTY);
+    if (curved)
+        bp_fdk_walk_kernel<true, NC><<<grid, block, 0, s>>>(T, proj, vol, view0, nviews, scale, accumulate);
+    else
+        bp_fdk_walk_kernel<false, NC><<<grid, block, 0, s>>>(T, proj, vol, view0, nviews, scale, accumulate);
+}
+
+static int fdk_orbit(const ctgb_params *p) {
+    if (CTGB_WALK_NC >= 4 && fdk_fourfold(p)) return 4;
+    if (CTGB_WALK_NC >= 2 && fdk_twofold(p)) return 2;
+    return 1;
+}
+
+extern "C" int ctgb_backproject_fdk_orbit_size(const ctgb_params *p, int32_t *nc) {
+    clear_error();
+    if (!p || !nc) return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_orbit_size: NULL argument");
+    *nc = fdk_orbit(p);
+    return CTGB_OK;
+}
+
+extern "C" int ctgb_backproject_fdk_orbits(const ctgb_params *p, const void *d_table, const float *d_proj,
+                                           float *d_vol, int32_t base0, int32_t nbase, float scale,
+                                           int32_t accumulate, void *stream) {
+    clear_error();
+    if (!p || !d_table || !d_vol || (!d_proj && nbase > 0))
+        return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_orbits: NULL argument");
+    const int nc = fdk_orbit(p), period = p->nviews / nc;
+    if (base0 < 0 || nbase < 0 || base0 + nbase > period)
+        return set_error(CTGB_ERR_ARG, "ctgb_backproject_fdk_orbits: base views [%d,%d) outside [0,%d)", base0,
+                         base0 + nbase, period);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nbase == 0) {
+        if (!accumulate) {
+            cudaError_t e = cudaMemsetAsync(d_vol, 0, sizeof(float) * (size_t)p->nx * p->ny * p->nz, s);
+            if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+        }
+        return CTGB_OK;
+    }
+    if ((long long)p->nu * (p->nv + 2) >= (1LL << 31))
+        return set_error(CTGB_ERR_SIZE, "ctgb_backproject_fdk_orbits: detector of %d x %d pixels too large", p->nu,
+                         p->nv);
+    const float *T = static_cast<const float *>(d_table);
+    if (nc == 4) {
+        const int hn = p->nx / 2;
+        dim3 grid((hn + kWkTX - 1) / kWkTX, (hn + kWkTY - 1) / kWkTY, (p->nz + WalkShape<4>::Z - 1) / WalkShape<4>::Z);
+        launch_walk<4>(p->curved, grid, s, T, d_proj, d_vol, base0, nbase, scale, accumulate);
+    } else if (nc == 2) {
+        dim3 grid((p->nx + kWkTX - 1) / kWkTX, (p->ny / 2 + kWkTY - 1) / kWkTY,
+                  (p->nz + WalkShape<2>::Z - 1) / WalkShape<2>::Z);
+        launch_walk<2>(p->curved, grid, s, T, d_proj, d_vol, base0, nbase, scale, accumulate);
+    } else {
+        dim3 grid((p->nx + kWkTX - 1) / kWkTX, (p->ny + kWkTY - 1) / kWkTY,
+                  (p->nz + WalkShape<1>::Z - 1) / WalkShape<1>::Z);
+        launch_walk<1>(p->curved, grid, s, T, d_proj + (long long)base0 * p->nu * p->nv, d_vol, base0, nbase, scale,
+                       accumulate);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_walk_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
 extern "C" int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                                     int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream) {
     clear_error();
@@ -1155,14 +1441,24 @@ extern "C" int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, c
         }
         return CTGB_OK;
     }
-    dim3 block(kBpTX, kBpTY);
-    dim3 grid((p->nx + kBpTX - 1) / kBpTX, (p->ny + kBpTY - 1) / kBpTY, (p->nz + kBpZ - 1) / kBpZ);
-    if (p->curved)
-        bp_fdk_table_kernel<true><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
-    else
-        bp_fdk_table_kernel<false><<<grid, block, 0, s>>>(T, d_proj, d_vol, view0, nviews, scale, accumulate);
+    if ((long long)p->nu * (p->nv + 2) >= (1LL << 31))
+        return set_error(CTGB_ERR_SIZE, "ctgb_backproject_fdk: detector of %d x %d pixels too large", p->nu, p->nv);
+    const bool full = view0 == 0 && nviews == p->nviews;
+    if (CTGB_WALK_NC >= 4 && full && fdk_fourfold(p)) {
+        const int hn = p->nx / 2;
+        dim3 grid((hn + kWkTX - 1) / kWkTX, (hn + kWkTY - 1) / kWkTY, (p->nz + WalkShape<4>::Z - 1) / WalkShape<4>::Z);
+        launch_walk<4>(p->curved, grid, s, T, d_proj, d_vol, 0, p->nviews / 4, scale, accumulate);
+    } else if (CTGB_WALK_NC >= 2 && full && fdk_twofold(p)) {
+        dim3 grid((p->nx + kWkTX - 1) / kWkTX, (p->ny / 2 + kWkTY - 1) / kWkTY,
+                  (p->nz + WalkShape<2>::Z - 1) / WalkShape<2>::Z);
+        launch_walk<2>(p->curved, grid, s, T, d_proj, d_vol, 0, p->nviews / 2, scale, accumulate);
+    } else {
+        dim3 grid((p->nx + kWkTX - 1) / kWkTX, (p->ny + kWkTY - 1) / kWkTY,
+                  (p->nz + WalkShape<1>::Z - 1) / WalkShape<1>::Z);
+        launch_walk<1>(p->curved, grid, s, T, d_proj, d_vol, view0, nviews, scale, accumulate);
+    }
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_table_kernel: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_fdk_walk_kernel: %s", cudaGetErrorString(e));
     return CTGB_OK;
 }
 
@@ -1206,6 +1502,10 @@ extern "C" int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table
         }
         return CTGB_OK;
     }
+    // A full orbit with four-fold symmetry runs the row walk over the raw
+    // projections (no workspace needed): faster than integrating them.
+    if (CTGB_WALK_NC >= 4 && view0 == 0 && nviews == p->nviews && fdk_fourfold(p))
+        return ctgb_backproject_fdk(p, d_table, d_proj, d_vol, view0, nviews, scale, accumulate, stream);
     const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
     const int chunk = (int)(workspace_bytes / per_view);
     if (chunk < 1) return set_error(CTGB_ERR_SIZE, "ctgb_backproject_fdk_ws: workspace below one view");

@@ -105,6 +105,24 @@ class Projector:
                       view0, nviews, sc, int(bool(accumulate)), _ptr(ws), ws.numel() * 4, _stream())
         return out
 
+    def orbit_size(self):
+        """Rotation-orbit size (4, 2 or 1) the FDK backprojector shares its
+        per-view set-up over for a call on every view of this scan."""
+        n = ctypes.c_int32(0)
+        _lib.call("ctgb_backproject_fdk_orbit_size", ctypes.byref(self.c), ctypes.byref(n))
+        return n.value
+
+    def backproject_fdk_orbits(self, proj, out, base0, nbase, scale=None, accumulate=False):
+        """backproject_fdk over base views [base0, base0 + nbase) of the
+        symmetric orbit (each base view b stands for the views b + k * views /
+        orbit_size()); proj holds every view of the scan."""
+        self._check(proj, self.proj_shape(), "proj")
+        self._check(out, self.volume_shape, "out")
+        sc = self.params.dtheta if scale is None else float(scale)
+        _lib.call("ctgb_backproject_fdk_orbits", ctypes.byref(self.c), _ptr(self.table), _ptr(proj), _ptr(out),
+                  int(base0), int(nbase), sc, int(bool(accumulate)), _stream())
+        return out
+
     def ray_forward(self, vol, out=None, view0=0, nviews=None):
         """Siddon ray sums to every pixel centre (the `Method: 'Ray'` projector)."""
         view0, nviews = self._views(view0, nviews)

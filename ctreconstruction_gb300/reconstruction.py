@@ -159,13 +159,28 @@ class Reconstruction:
             raise ValueError("proj must have shape %s, got %s" % (shape, tuple(src.shape)))
         q = self._device_buffer("proj_in", shape)
         vol = torch.empty(P.volume_shape, dtype=torch.float32, device=P.device)
-        for i, (v0, n) in enumerate(self._chunks(shape[0])):
+        # Symmetric orbits: each chunk is a range of base views, whose nc
+        # slabs (one per 1/nc turn) are copied before its launch.
+        nc = P.orbit_size()
+        if nc == 1:
+            for i, (v0, n) in enumerate(self._chunks(shape[0])):
+                with torch.cuda.stream(copy):
+                    q[v0:v0 + n].copy_(src[v0:v0 + n], non_blocking=True)
+                landed = torch.cuda.Event()
+                landed.record(copy)
+                compute.wait_event(landed)
+                P.backproject_fdk(q[v0:v0 + n], out=vol, view0=v0, nviews=n, accumulate=i > 0)
+            return self._to_host(vol, src, "image")
+        period = shape[0] // nc
+        for i, (b0, n) in enumerate(self._chunks(period)):
             with torch.cuda.stream(copy):
-                q[v0:v0 + n].copy_(src[v0:v0 + n], non_blocking=True)
+                for k in range(nc):
+                    v0 = b0 + k * period
+                    q[v0:v0 + n].copy_(src[v0:v0 + n], non_blocking=True)
             landed = torch.cuda.Event()
             landed.record(copy)
             compute.wait_event(landed)
-            P.backproject_fdk(q[v0:v0 + n], out=vol, view0=v0, nviews=n, accumulate=i > 0)
+            P.backproject_fdk_orbits(q, vol, b0, n, accumulate=i > 0)
         return self._to_host(vol, src, "image")
 
     # -- projectors ----------------------------------------------------------------

@@ -106,15 +106,37 @@ int ctgb_transpose_xy(const float *d_vol, float *d_vol_xzy, int32_t nx, int32_t 
  * :261-271, :371-482) and flat_/curved_distance_backproj_arb
  * (GPUFuncs_numba.py:391-686; GPUFuncs_pycuda.py:837-956 flat_..._arb2).
  * vol = (accumulate ? vol : 0) + scale * sum_v BP_v(proj[v-view0]) where the
- * reference's backward() uses scale = dtheta = angle[1]-angle[0]. */
+ * reference's backward() uses scale = dtheta = angle[1]-angle[0].
+ * No workspace: each voxel column walks up the detector rows under its
+ * footprint once per view.  A call over every view of a full circular orbit
+ * whose view count is a multiple of 4 (or 2), with a square (or even-height)
+ * grid centred on the rotation axis and no helical pitch, computes each
+ * (column, view) set-up once for the 4 (or 2) columns that a quarter (half)
+ * turn maps onto each other. */
 int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                          int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *stream);
+/* ctgb_backproject_fdk over part of a symmetric orbit, for callers that feed
+ * the views in pieces (e.g. while they arrive from host memory).
+ * ctgb_backproject_fdk_orbit_size gives nc = 4, 2 or 1, the rotation-orbit
+ * size that ctgb_backproject_fdk uses for a call over every view; the views
+ * then split into base views b in [0, nviews/nc), and base view b stands for
+ * the nc views b + k * nviews/nc.  ctgb_backproject_fdk_orbits backprojects
+ * base views [base0, base0 + nbase): d_proj holds every view of the scan (at
+ * least those nc slabs), indexed by absolute view.  Calls over base ranges
+ * that tile [0, nviews/nc), the first with accumulate = 0 and the rest with
+ * 1, give ctgb_backproject_fdk's result up to float summation order.
+ * Replaces the same reference code as ctgb_backproject_fdk. */
+int ctgb_backproject_fdk_orbit_size(const ctgb_params *p, int32_t *nc);
+int ctgb_backproject_fdk_orbits(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
+                                int32_t base0, int32_t nbase, float scale, int32_t accumulate, void *stream);
 
-/* Same result as ctgb_backproject_fdk, faster: the projections are first
- * integrated along v into a caller-supplied workspace of float2 (running sum,
- * value) per detector cell and view, so each voxel's footprint costs two
- * lookups per detector column.  Views are processed in chunks that fit the
- * workspace (at least one view: ctgb_backproject_fdk_workspace_bytes(p, 1, ..)).
+/* Same result as ctgb_backproject_fdk: the projections are first integrated
+ * along v into a caller-supplied workspace of float2 (running sum, value) per
+ * detector cell and view, so each voxel's footprint costs two lookups per
+ * detector column.  Views are processed in chunks that fit the workspace (at
+ * least one view: ctgb_backproject_fdk_workspace_bytes(p, 1, ..)).  A call
+ * that ctgb_backproject_fdk serves with four-fold symmetry goes there
+ * instead (it is faster) and leaves the workspace untouched.
  * Replaces the same reference code as ctgb_backproject_fdk. */
 /* Workspace bytes for nviews views of ctgb_backproject_fdk_ws and of
  * ctgb_backproject_matched_ws (the latter's per-view tables included). */

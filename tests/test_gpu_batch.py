@@ -3,7 +3,8 @@ of uneven sizes advanced by single persistent launches with the drivers'
 residual and update lines fused into the projectors' stores, against the same
 single-scan solvers run one by one with separate element-wise kernels.  The
 fused epilogues evaluate the same expressions, so the iterates agree bit for
-bit."""
+bit (to float summation order where a single scan's FDK backprojection takes
+the row walk of a quarter-turn-symmetric orbit)."""
 import numpy as np
 import pytest
 import torch
@@ -60,6 +61,13 @@ def test_batched_solver_matches_solvers_one_by_one(cuda, scans, kind):
     b.run(3)
     torch.cuda.synchronize()
     for a, c in zip(ref, b.solvers):
+        if kind != "ossart" and a.P.orbit_size() == 4:
+            # a single scan on a quarter-turn-symmetric orbit backprojects by
+            # the row walk, the batch by integrated projections: the same sums
+            # in another float order
+            err = float((a.x - c.x).abs().max() / a.x.abs().max())
+            assert err < 1e-5, (kind, err)
+            continue
         assert torch.equal(a.x, c.x), kind
         if kind == "mlem":   # EM.py zeroes measured data where A x == 0, in place
             assert torch.equal(a.proj0, c.proj0)

@@ -85,6 +85,28 @@ def test_cfg3_fdk_backprojection_slabs(cfg3):
     assert max(errs.values()) <= RTOL, errs
 
 
+def test_cfg3_fdk_walk_full_orbit(cfg3):
+    """The benchmark's backward(): one row-walk launch over all 720 views
+    sharing each set-up between the four columns of a quarter-turn orbit.  The
+    whole volume against the integrated-projection kernel (pinned per view
+    above), and the central 8-slice slab against the FP64 oracle over all 720
+    views."""
+    p, P, vol = cfg3
+    assert P.orbit_size() == 4
+    proj = P.forward(vol)
+    got = P.backproject_fdk(proj)
+    integ = P.integrate(proj)
+    ref = P.backproject_fdk_integrated(integ)
+    errs = {"vs_integrated": float((got - ref).abs().max() / ref.abs().max())}
+    del integ, ref
+    z0 = 252
+    g = OracleGeometry(slab_params(p, z0, 8).as_dict())
+    want = g.backward_fdk(proj.cpu().numpy())
+    errs["vs_oracle_z%d" % z0] = rel_err(got[z0:z0 + 8].cpu().numpy(), want)
+    _report("backproject_fdk_walk", errs)
+    assert max(errs.values()) <= RTOL, errs
+
+
 # Single-view matched backprojections at oblique views carry the float32
 # rounding of the detector columns' transverse footprint positions: on a
 # 512-voxel grid a boundary ray's position (a difference of two terms near
