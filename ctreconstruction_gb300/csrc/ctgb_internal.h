@@ -2,6 +2,7 @@
 // table builder (geometry.cpp) and the CUDA kernels.
 #pragma once
 #include <stdint.h>
+#include <vector>
 #include "../../include/ctgb.h"
 
 namespace ctgb {
@@ -68,5 +69,18 @@ ViewOffsets view_offsets(int nu, int nv) {
     o.stride = (o.stride + 31) & ~int64_t(31);  // 128-byte aligned records
     return o;
 }
+
+// A full circular orbit whose view count is a multiple of 4 (float32 cosines
+// and sines repeat, rotated, every quarter of the views): the geometry table
+// then holds views v + views/4 as exact quarter-turn rotations of view v
+// (geometry.cpp), except in the view groups {g + k views/4} listed in
+// *broken, where the forward's dominant axis does not alternate between x
+// and y (45-degree ties).
+bool quarter_turn_views(const ctgb_params *p, std::vector<int> *broken);
+// The forward's slice centres (plane + half a spacing, in float) of a square
+// grid are exact negatives of each other under the reflections a quarter
+// turn makes (x_i = y_(n-1-i) = -x_(n-1-i) = -y_i), so the four views of a
+// rotation group see their slices at exactly +-the same source distance.
+bool slice_centres_antisymmetric(const ctgb_params *p);
 
 }  // namespace ctgb

@@ -963,7 +963,7 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
 // factors 1 / (Sa - Pa[c]) for c = 0 .. nu - 1, written once here with the
 // forward's expressions so the backprojector's candidate search reads them
 // instead of dividing per voxel column (the search was most of its time).
-__device__ __forceinline__ int matched_tab_stride(int nu) { return 2 * nu + 2; }
+__host__ __device__ __forceinline__ int matched_tab_stride(int nu) { return 2 * nu + 2; }
 
 // Column c of view vi (t = vi * nu + c) of the matched backprojector's
 // integration pass.
@@ -1191,6 +1191,238 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
                           const float b = __fmul_rn(scale, a);
                           vol[i] = accumulate ? __fadd_rn(vol[i], b) : b;
                       });
+}
+
+// ---------------------------------------------------------------------------
+// Matched backprojection over a quarter-turn-symmetric orbit.
+//
+// With a square grid centred on the rotation axis, forward planes centred
+// there too and a full circular orbit whose view count is a multiple of 4
+// (the conditions of the FDK walk's orbits), the forward projector's
+// geometry of column (x, y) at view v is that of column (-y, x) at view
+// v + Q (Q = views / 4): the same slice distance, candidate detector columns,
+// transverse overlaps and row placement (to float rounding of the table's
+// per-view values, which a quarter turn maps onto each other).  A thread
+// owns the four columns of one rotation orbit (the grid covers a quadrant):
+// per set-up view it searches the candidate columns and places their rows
+// once, and per z boundary it computes the row coordinate, floor and
+// fraction once; only the four (C, y') lookups and sums are per column.
+// The integrated projections of every view are in the workspace (absolute
+// view index), so each column reads its own view v + k Q.
+// At 512^3 / 720 views: 12 voxels per chunk at 4 CTAs per SM (128
+// registers) 137.9 ms; 8 at 5 155.1, 8 at 6 260.1 and 12 at 5 288.0 (both
+// spill in the lookup loop), 16 at 4 296.8.
+#ifndef CTGB_MO_Z
+#define CTGB_MO_Z 12
+#endif
+#ifndef CTGB_MO_B
+#define CTGB_MO_B 4
+#endif
+constexpr int kMoZ = CTGB_MO_Z;
+
+__global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MO_B)
+bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
+                        const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
+                        float scale, int accumulate) {
+    // Candidate columns of the current set-up view, per thread (registers
+    // held them across the lookup loop at the cost of spills).
+    __shared__ float cand[7][kMC][kMiTX * kMiTY];   // column, 4 weights, tau, 1 / (tau dB)
+    const int tid = threadIdx.y * kMiTX + threadIdx.x;
+    const TableHeader &h = header(T);
+    const int n = h.nx, hn = n / 2, n1 = n - 1;
+    const int ix = blockIdx.x * kMiTX + threadIdx.x;
+    const int iy = blockIdx.y * kMiTY + threadIdx.y;
+    const int l0 = blockIdx.z * kMoZ;
+    const bool live = ix < hn && iy < hn;
+    const int ixc = min(ix, n1), iyc = min(iy, n1);
+    const int nu = h.nu, nv = h.nv, nz = h.nz, nall = h.nviews, Q = nall / 4;
+    const ViewOffsets vo = view_offsets(nu, nv);
+    const float inv_dz = 1.0f / h.dz;
+    const float fnv = (float)nv;
+    const long long istride = (long long)(nv + 1) * nu;
+    // orbit columns: (i, j), (j, n-1-i), (n-1-i, n-1-j), (n-1-j, i)
+    auto ocx = [&](int k) { return k == 0 ? ixc : k == 1 ? iyc : k == 2 ? n1 - ixc : n1 - iyc; };
+    auto ocy = [&](int k) { return k == 0 ? iyc : k == 1 ? n1 - ixc : k == 2 ? n1 - iyc : ixc; };
+    float acc[4][kMoZ];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int j = 0; j < kMoZ; ++j) acc[k][j] = 0.0f;
+
+#pragma unroll 1
+    for (int sv = 0; sv < nall; ++sv) {
+        int pv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int v = sv + k * Q;
+            pv[k] = v < nall ? v : v - nall;
+        }
+        const float *__restrict__ pzp = T + h.off_zplane;
+        const float *__restrict__ V = T + h.off_views + (long long)sv * h.view_stride;
+        const int axis = (int)V[VF_AXIS];
+        // A group whose dominant axis does not alternate (45-degree ties) is
+        // backprojected view by view by the host's follow-up launches.
+        bool group_ok = true;
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+            group_ok = group_ok && (int)T[h.off_views + (long long)pv[k] * h.view_stride + VF_AXIS] == (axis ^ (k & 1));
+        if (!group_ok) continue;
+        if (axis == 2) {
+            // z-dominant (not on a circular orbit): per-voxel search per column
+            if (!live) continue;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float *__restrict__ Vk = T + h.off_views + (long long)pv[k] * h.view_stride;
+                const float *__restrict__ Qk = proj + (long long)pv[k] * nu * nv;
+                const int ak = (int)Vk[VF_AXIS];
+#pragma unroll
+                for (int j = 0; j < kMoZ; ++j) {
+                    if (l0 + j >= nz) continue;
+                    acc[k][j] += ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
+                               : ak == 1 ? matched_voxel_view<1>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
+                                         : matched_voxel_view<2>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j);
+                }
+            }
+            continue;
+        }
+        const bool xd = axis == 0;
+        const int s = xd ? ixc : iyc, kk = xd ? iyc : ixc;
+        const float *__restrict__ pa = T + (xd ? h.off_xplane : h.off_yplane);
+        const float *__restrict__ pb = T + (xd ? h.off_yplane : h.off_xplane);
+        const float da = xd ? h.dx : h.dy;
+        const float Sz = V[VF_SZ];
+        const float A = (Sz - pzp[0]) * inv_dz;
+        const float q = pa[s] + 0.5f * da - (xd ? V[VF_SX] : V[VF_SY]);
+        const float B0 = V[VF_B0], dB = V[VF_DB];
+        // Per orbit column k (view sv + k Q, dominant axis alternating): the
+        // forward's own transverse frame.  The slice distance is +-q exactly
+        // (the host checks the slice centres' antisymmetry), so 1/q^2, the
+        // depth factor tau and the row placement are shared; the transverse
+        // coordinate x = Eb q + Cb and its overlap with cell kk are evaluated
+        // per column with that view's expressions (as mirror images they
+        // round differently).
+        float qk[4], cbk[4], kfk[4], gk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool xdk = (axis ^ (k & 1)) == 0;
+            const float *__restrict__ Vk = T + h.off_views + (long long)pv[k] * h.view_stride;
+            const int cxk = ocx(k), cyk = ocy(k);
+            const int sk = xdk ? cxk : cyk;
+            const float *__restrict__ pak = T + (xdk ? h.off_xplane : h.off_yplane);
+            const float *__restrict__ pbk = T + (xdk ? h.off_yplane : h.off_xplane);
+            const float dak = xdk ? h.dx : h.dy, dbk = xdk ? h.dy : h.dx;
+            const float Sak = xdk ? Vk[VF_SX] : Vk[VF_SY], Sbk = xdk ? Vk[VF_SY] : Vk[VF_SX];
+            qk[k] = pak[sk] + 0.5f * dak - Sak;
+            cbk[k] = (Sbk - pbk[0]) * (1.0f / dbk);
+            kfk[k] = (float)(xdk ? cyk : cxk);
+            gk[k] = 1.0f / (qk[k] * qk[k]);
+        }
+        float cmin = INFINITY, cmax = -INFINITY;
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float bw = pb[kk + e];
+            const float pcw = pa[s] + 0.5f * da;
+            const float ddx = (xd ? pcw : bw) - V[VF_SX];
+            const float ddy = (xd ? bw : pcw) - V[VF_SY];
+            const float aa = ddx * V[VF_EUX] + ddy * V[VF_EUY], bb = ddx * V[VF_EWX] + ddy * V[VF_EWY];
+            const float u = h.curved ? atan2f(aa, bb) : h.sdd * aa / bb;
+            const float cu = (u - h.u0_fwd) / h.du_fwd;
+            cmin = fminf(cmin, cu); cmax = fmaxf(cmax, cu);
+        }
+        const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
+        const float *__restrict__ EbT = tabs + (long long)sv * matched_tab_stride(nu);
+        const float *__restrict__ IPT = EbT + nu + 1;
+        int ncol = 0;
+        bool overflow = false;
+        for (int c = cA; c <= cB; ++c) {
+            const float Eb0 = __ldg(EbT + c), Eb1 = __ldg(EbT + c + 1);
+            float ovk[4];
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float xa = fmaf(Eb0, qk[k], cbk[k]), xb = fmaf(Eb1, qk[k], cbk[k]);
+                const float o = fminf(kfk[k] + 1.0f, fmaxf(xa, xb)) - fmaxf(kfk[k], fminf(xa, xb));
+                ovk[k] = o > 0.0f ? o : 0.0f;
+                any = any || o > 0.0f;
+            }
+            if (!any) continue;
+            const float tau = q * __ldg(IPT + c);
+            const float inv = 1.0f / (tau * dB);
+            const float wz = fabsf(dB * tau);
+            if (ncol < kMC) {
+                cand[0][ncol][tid] = __int_as_float(c);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) cand[1 + k][ncol][tid] = ovk[k] * gk[k] * wz;
+                cand[5][ncol][tid] = tau;
+                cand[6][ncol][tid] = inv;
+                ++ncol;
+            } else {
+                overflow = true;
+            }
+        }
+        if (!live) continue;
+        if (overflow) {
+            // Detector columns much narrower than a voxel: per-voxel search per column.
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float *__restrict__ Vk = T + h.off_views + (long long)pv[k] * h.view_stride;
+                const float *__restrict__ Qk = proj + (long long)pv[k] * nu * nv;
+                const int ak = (int)Vk[VF_AXIS];
+#pragma unroll
+                for (int j = 0; j < kMoZ; ++j) {
+                    if (l0 + j >= nz) continue;
+                    acc[k][j] += ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
+                                         : matched_voxel_view<1>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j);
+                }
+            }
+            continue;
+        }
+        const float b0r = B0 / dB;
+#pragma unroll 1
+        for (int m = 0; m < ncol; ++m) {
+            // candidate m: the same row placement as bp_matched_column
+            const int cm = __float_as_int(cand[0][m][tid]);
+            const float tm = cand[5][m][tid], bm = cand[6][m][tid];
+            float wk[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) wk[k] = bm > 0.0f ? cand[1 + k][m][tid] : -cand[1 + k][m][tid];
+            const int R = min(max((int)floorf(fmaf((float)l0 - A, bm, -b0r)), 0), nv);
+            const ZFrame zf = row_frame(A, tm, B0, dB, (float)R);
+            const float d0 = ((float)l0 - zf.ibf) - zf.f;
+            const float rlo = -(float)R, rhi = fnv - (float)R;
+            int coff[4];   // element offsets of the four views' column cm (< 2^31, checked by the host)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) coff[k] = pv[k] * (int)istride + cm;
+            float eprev[4];
+#pragma unroll
+            for (int j = 0; j <= kMoZ; ++j) {
+                const float rr = fminf(fmaxf((d0 + (float)j) * bm, rlo), rhi);
+                float fr;
+                const int mr = R + floor_split(rr, &fr);
+                const int off = mr * nu;
+                const float fx = rr - fr;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float2 a = __ldg(integ + (coff[k] + off));
+                    const float e = fmaf(a.y, fx, a.x);
+                    if (j > 0) acc[k][j - 1] = fmaf(e - eprev[k], wk[k], acc[k][j - 1]);
+                    eprev[k] = e;
+                }
+            }
+        }
+    }
+    if (!live) return;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int j = 0; j < kMoZ; ++j) {
+            const int iz = l0 + j;
+            if (iz < nz) {
+                float *dst = vol + ((long long)iz * n + ocy(k)) * n + ocx(k);
+                const float b = __fmul_rn(scale, acc[k][j]);
+                *dst = accumulate ? __fadd_rn(*dst, b) : b;
+            }
+        }
 }
 
 // ---- batched backprojection (many scans per launch) --------------------------
@@ -1588,6 +1820,37 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
     const float *T = static_cast<const float *>(d_table);
     float2 *ws = static_cast<float2 *>(d_workspace);
     dim3 block(kMiTX, kMiTY);
+    // A full quarter-turn-symmetric orbit whose integrated views all fit the
+    // workspace: one integration pass, then the orbit kernel.
+    // Needs the table's exactly rotated view records (quarter_turn_views) and
+    // a square grid of even side whose forward planes are centred on the axis.
+    const double *cf = p->flavour == CTGB_FLAVOUR_PYCUDA ? p->recon_center : p->phantom_center;
+    const bool square = p->nx == p->ny && !(p->nx & 1) && p->dx == p->dy && cf[0] == 0.0 && cf[1] == 0.0 &&
+                        slice_centres_antisymmetric(p);
+    std::vector<int> broken;
+    if (CTGB_WALK_NC >= 4 && view0 == 0 && nviews == p->nviews && chunk >= nviews && square &&
+        (long long)p->nviews * (p->nv + 1) * p->nu < (1LL << 31) && quarter_turn_views(p, &broken)) {
+        const long long threads = (long long)p->nu * nviews;
+        float *tabs = reinterpret_cast<float *>(ws + (size_t)nviews * (p->nv + 1) * p->nu);
+        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, d_proj, ws, tabs, 0, nviews);
+        const int hn = p->nx / 2;
+        dim3 ogrid((hn + kMiTX - 1) / kMiTX, (hn + kMiTY - 1) / kMiTY, (p->nz + kMoZ - 1) / kMoZ);
+        bp_matched_orbit_kernel<<<ogrid, block, 0, s>>>(T, ws, tabs, d_proj, d_vol, scale, accumulate);
+        // the views of groups the orbit kernel skipped, one launch each
+        const int q = nviews / 4;
+        const size_t rows_elems = (size_t)(p->nv + 1) * p->nu;
+        dim3 grid1((p->nx + kMiTX - 1) / kMiTX, (p->ny + kMiTY - 1) / kMiTY, (p->nz + kMZ - 1) / kMZ);
+        for (int g : broken)
+            for (int k = 0; k < 4; ++k) {
+                const int v = g + k * q;
+                bp_matched_integ_kernel<<<grid1, block, 0, s>>>(
+                    T, ws + (size_t)v * rows_elems, tabs + (size_t)v * matched_tab_stride(p->nu),
+                    d_proj + (long long)v * p->nu * p->nv, d_vol, v, 1, scale, 1);
+            }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_orbit_kernel: %s", cudaGetErrorString(e));
+        return CTGB_OK;
+    }
     dim3 grid((p->nx + kMiTX - 1) / kMiTX, (p->ny + kMiTY - 1) / kMiTY, (p->nz + kMZ - 1) / kMZ);
     for (int v = 0; v < nviews; v += chunk) {
         const int n = nviews - v < chunk ? nviews - v : chunk;

@@ -70,6 +70,53 @@ static Scan scan_of(const ctgb_params *p) {
     return s;
 }
 
+// Dominant axis of the forward projector at view angle th
+// (distance_forward, python/Reconstruction_numba.py:896, :966).
+static int view_axis(const ctgb_params *p, const Scan &s, double th) {
+    const double zs = s.H * th / (2 * M_PI);
+    const double S[3] = {-s.sad * std::sin(th), s.sad * std::cos(th), p->source_init[2] + zs};
+    const double D[3] = {(s.sdd - s.sad) * std::sin(th), -(s.sdd - s.sad) * std::cos(th), p->detector_init[2] + zs};
+    const double ax = std::fabs(S[0] - D[0]), ay = std::fabs(S[1] - D[1]), az = std::fabs(S[2] - D[2]);
+    return (ax >= ay && ax >= az) ? 0 : (ay >= ax && ay >= az) ? 1 : 2;
+}
+
+bool quarter_turn_views(const ctgb_params *p, std::vector<int> *broken) {
+    const int n = p->nviews, q = n / 4;
+    if (broken) broken->clear();
+    if (n < 4 || n % 4 || p->pitch != 0.0) return false;
+    const Scan s = scan_of(p);
+    std::vector<char> bad(q, 0);
+    for (int v = 0; v < n; ++v) {
+        const int w = (v + q) % n;
+        const double a = s.angles[v], b = s.angles[w];
+        const float ca = (float)std::cos(a), sa = (float)std::sin(a), cb = (float)std::cos(b), sb = (float)std::sin(b);
+        if (std::fabs(cb + sa) > 2.4e-7f || std::fabs(sb - ca) > 2.4e-7f) return false;
+        const int xa = view_axis(p, s, a), xb = view_axis(p, s, b);
+        if (xa == 2 || xb != 1 - xa) bad[v % q] = 1;
+    }
+    if (broken)
+        for (int g = 0; g < q; ++g)
+            if (bad[g]) broken->push_back(g);
+    return true;
+}
+
+bool slice_centres_antisymmetric(const ctgb_params *p) {
+    if (p->nx != p->ny || p->dx != p->dy) return false;
+    const bool pyc = p->flavour == CTGB_FLAVOUR_PYCUDA;
+    const double *C = pyc ? p->recon_center : p->phantom_center;
+    const int n = p->nx;
+    const double dx = p->dx, dy = -p->dy;
+    const float fdx = (float)dx, fdy = (float)dy;
+    // the forward's slice centres as the kernels form them: plane + 0.5f * spacing
+    auto fx = [&](int i) { return (float)(C[0] + (i - (n - 1) / 2.0) * dx - dx / 2) + 0.5f * fdx; };
+    auto fy = [&](int i) { return (float)(C[1] + (i - (n - 1) / 2.0) * dy - dy / 2) + 0.5f * fdy; };
+    for (int i = 0; i < n; ++i) {
+        const float a = fx(i);
+        if (fy(n - 1 - i) != a || fx(n - 1 - i) != -a || fy(i) != -a) return false;
+    }
+    return true;
+}
+
 }  // namespace ctgb
 
 using namespace ctgb;
@@ -185,6 +232,33 @@ extern "C" int ctgb_table_build(const ctgb_params *p, void *host_table, size_t b
         for (int r = 0; r < nv; ++r) {
             double z = pyc ? S[2] + ((r - (nv - 1) / 2.0) * -p->dv + voff) : S[2] - (r - (nv - 1) / 2.0) * p->dv;
             V[vo.pz + r] = (float)z;
+        }
+    }
+    // A full circular orbit with a view count divisible by 4: rebuild views
+    // v + Q (Q = views / 4) as exact quarter-turn rotations, (x, y) -> (-y, x),
+    // of view v's float values, except in groups {g + k Q} where the forward's
+    // dominant axis does not alternate (45-degree views, where the reference's
+    // tie-break slices two views of the group along x).  Independently rounded, the two records differ
+    // by an ulp (6e-5 mm at a 1000 mm source distance, 1e-4 of a detector
+    // pixel); rotated exactly, every float expression of the forward projector
+    // gives view v + Q the numbers it gives view v, so the matched
+    // backprojector may share set-ups between the columns of a rotation orbit
+    // and still be the forward's exact transpose.
+    std::vector<int> broken;
+    if (quarter_turn_views(p, &broken)) {
+        const int q = p->nviews / 4;
+        std::vector<char> bad(q, 0);
+        for (int g : broken) bad[g] = 1;
+        for (int v = q; v < p->nviews; ++v) {
+            if (bad[v % q]) continue;   // a 45-degree tie: the reference slices both views along x
+            const float *A = T + h.off_views + (int64_t)(v - q) * h.view_stride;
+            float *V = T + h.off_views + (int64_t)v * h.view_stride;
+            V[VF_SX] = -A[VF_SY]; V[VF_SY] = A[VF_SX];
+            V[VF_COS] = -A[VF_SIN]; V[VF_SIN] = A[VF_COS];
+            V[VF_EUX] = -A[VF_EUY]; V[VF_EUY] = A[VF_EUX];
+            V[VF_EWX] = -A[VF_EWY]; V[VF_EWY] = A[VF_EWX];
+            for (int c = 0; c <= nu; ++c) { V[vo.bx + c] = -A[vo.by + c]; V[vo.by + c] = A[vo.bx + c]; }
+            for (int c = 0; c < nu; ++c) { V[vo.px + c] = -A[vo.py + c]; V[vo.py + c] = A[vo.px + c]; }
         }
     }
     std::memcpy(host_table, &h, sizeof h);

@@ -61,6 +61,11 @@ typedef struct ctgb_params {
  * :405-413) is built once, in float64 on the host, into a flat table that the
  * caller copies to device memory and passes to the projectors. */
 int ctgb_table_bytes(const ctgb_params *p, size_t *bytes);
+/* On a full circular orbit whose view count is a multiple of 4, the view
+ * records v + nviews/4 are stored as exact quarter-turn rotations of view v's
+ * float values (rather than rounded independently, which differs by an ulp),
+ * except in the groups of views containing a 45-degree tie of the forward's
+ * dominant axis; the symmetric backprojectors rely on this. */
 int ctgb_table_build(const ctgb_params *p, void *host_table, size_t bytes);
 
 /* ---- DD forward projection -------------------------------------------------

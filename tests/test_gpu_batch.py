@@ -3,8 +3,8 @@ of uneven sizes advanced by single persistent launches with the drivers'
 residual and update lines fused into the projectors' stores, against the same
 single-scan solvers run one by one with separate element-wise kernels.  The
 fused epilogues evaluate the same expressions, so the iterates agree bit for
-bit (to float summation order where a single scan's FDK backprojection takes
-the row walk of a quarter-turn-symmetric orbit)."""
+bit (to float rounding where a single scan's backprojection runs over the
+rotation orbits of a quarter-turn-symmetric scan)."""
 import numpy as np
 import pytest
 import torch
@@ -97,6 +97,12 @@ def test_batched_mlem_matched_backprojector(cuda, scans):
     b.run(2)
     torch.cuda.synchronize()
     for a, c in zip(ref, b.solvers):
+        if a.P.orbit_size() == 4:
+            # single scan: the quarter-turn orbit kernel (shared set-ups, the
+            # same float expressions otherwise); batch: one column per thread
+            err = float((a.x - c.x).abs().max() / a.x.abs().max())
+            assert err < 1e-5, err
+            continue
         assert torch.equal(a.x, c.x)
 
 
