@@ -1452,7 +1452,10 @@ struct IntegJob {
 
 // The batched bodies need more registers than the single-scan ones (at eight
 // or six CTAs per SM they spilled 700 and 270 bytes): four CTAs per SM.
-constexpr int kBatchBpBlocks = 4;
+#ifndef CTGB_BATCH_BP_BLOCKS
+#define CTGB_BATCH_BP_BLOCKS 4
+#endif
+constexpr int kBatchBpBlocks = CTGB_BATCH_BP_BLOCKS;
 
 template <bool CURVED>
 __global__ void __launch_bounds__(kBiTX * kBiTY, kBatchBpBlocks)

@@ -106,6 +106,46 @@ def test_dominant_axis_ties_break_like_the_reference():
     assert ties >= 1
 
 
+def test_quarter_turn_views_are_exact_rotations():
+    """On a full circular orbit with a view count divisible by 4 the table
+    stores view v + n/4 as the exact rotation (x, y) -> (-y, x) of view v's
+    float values, except in groups whose dominant axis does not alternate (the
+    45-degree views, where the reference's tie-break slices along x twice):
+    the symmetric backprojectors share set-ups across those groups."""
+    from _util import cfg3_params
+    p = cfg3_params(NumberOfImage=[8, 8, 8], NumberOfDetectorPixels=[16, 8])
+    buf = _table(p)
+    h = _header(buf)
+    nu, n, q = 16, 720, 180
+    rec = lambda v: buf[h["off_views"] + v * h["view_stride"]:h["off_views"] + (v + 1) * h["view_stride"]]
+    bx, by = 16, 16 + nu + 1                  # Bx[nu+1], By[nu+1] after the 16 scalars
+    axes = [int(rec(v)[0]) for v in range(n)]
+    broken = {g for g in range(q) if any(axes[(g + (k + 1) * q) % n] != 1 - axes[g + k * q] for k in range(3))}
+    assert broken == {90}                     # the 45-degree group: views 90, 270, 450, 630
+    for v in range(q, n):
+        if v % q in broken:
+            continue
+        a, b = rec(v - q), rec(v)
+        assert b[1] == -a[2] and b[2] == a[1], v                        # source x, y
+        assert np.array_equal(b[bx:bx + nu + 1], -a[by:by + nu + 1]), v  # column boundaries
+        assert np.array_equal(b[by:by + nu + 1], a[bx:bx + nu + 1]), v
+
+
+@pytest.mark.parametrize("over,nc", [({}, 4), ({'NumberOfImage': [12, 10, 8]}, 2), ({'NumberOfViews': 18}, 2),
+                                     ({'ReconCenter': [0.5, 0.0, 0.0]}, 1), ({'Pitch': 0.5}, 1),
+                                     ({'EndAngle': np.pi + 0.4}, 1), ({'NumberOfImage': [11, 12, 8]}, 2),
+                                     ({'NumberOfImage': [11, 11, 8]}, 1)])
+def test_fdk_orbit_size(over, nc):
+    """The rotation-orbit size the FDK backprojector can share set-ups over:
+    4 for a square grid of even side centred on the axis on a full orbit of
+    4k views, 2 for an even-height grid (or 4k + 2 views), 1 otherwise."""
+    p = cone_params(n=12, nviews=16, nu=20, nv=16, **over)
+    c = ReconstructionParams.from_dict(p, None).to_ctgb()
+    got = ctypes.c_int32(0)
+    _lib.call("ctgb_backproject_fdk_orbit_size", ctypes.byref(c), ctypes.byref(got))
+    assert got.value == nc
+
+
 def test_table_rejects_bad_geometry():
     p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
     p.nu = 0
