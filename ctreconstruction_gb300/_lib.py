@@ -105,6 +105,7 @@ SIGNATURES = {
     "ctgb_filter_build": [_P, _i32, ctypes.c_double, _vp, _sz],
     "ctgb_fdk_filter": [_P, _vp, _vp, _i32, _vp],
     "ctgb_device_status": [ctypes.POINTER(_i32), _i32],
+    "ctgb_selftest_bounded_wait": [_i32, _vp],
     "ctgb_partials_count": [ctypes.c_int64, ctypes.POINTER(_i32)],
     "ctgb_sart_residual": [_vp, _vp, _vp, _f32, _vp, ctypes.c_int64, _vp],
     "ctgb_sart_update": [_vp, _vp, _vp, _f32, _f32, _vp, ctypes.c_int64, _vp],

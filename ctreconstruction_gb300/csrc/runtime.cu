@@ -86,6 +86,32 @@ bool ctgb_make_tmap_bf16(CUtensorMap *map, const void *base, int rank, const uin
     return r == CUDA_SUCCESS;
 }
 
+// Self-test of the bounded device waits: one warp initialises an mbarrier
+// that expects one arrival, never arrives, and waits on it with a limit of
+// `polls` polls; the wait runs out, records kDevErrTimeout in the status word
+// and the kernel returns.  No copy is in flight and nothing else waits.
+__global__ void bounded_wait_selftest_kernel(long long polls, int *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        ctgb::mbar_init(&bar, 1);
+        ctgb::fence_mbar_init();
+    }
+    __syncwarp();
+    ctgb::mbar_wait(&bar, 0, status, polls);
+}
+
+extern "C" int ctgb_selftest_bounded_wait(int32_t polls, void *stream) {
+    ctgb::clear_error();
+    if (polls < 1 || polls > (1 << 20))
+        return ctgb::set_error(CTGB_ERR_ARG, "ctgb_selftest_bounded_wait: polls %d outside [1, 2^20]", polls);
+    int *status = ctgb_status_ptr();
+    if (!status) return ctgb::set_error(CTGB_ERR_CUDA, "ctgb_selftest_bounded_wait: device status word unavailable");
+    bounded_wait_selftest_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(polls, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return ctgb::set_error(CTGB_ERR_CUDA, "bounded_wait_selftest_kernel: %s", cudaGetErrorString(e));
+    return CTGB_OK;
+}
+
 // Reads (and optionally clears) the device status word of the current device.
 // Synchronises the device.  *out = 0 when no kernel reported a problem.
 extern "C" int ctgb_device_status(int32_t *out, int32_t clear) {

@@ -39,9 +39,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 
 // Bounded wait for the phase with the given parity; false on timeout (and
 // kDevErrTimeout is or-ed into *status, the library's device status word).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status,
+                                          long long limit = kWaitLimit) {
     const uint32_t a = smem_addr(bar);
-    for (long long i = 0; i < kWaitLimit; ++i) {
+    for (long long i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"

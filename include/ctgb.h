@@ -449,6 +449,12 @@ int ctgb_batch_backproject(const void *host_plan, const void *d_plan, int32_t ct
 #define CTGB_DEVERR_TIMEOUT 1
 #define CTGB_DEVERR_ARG 2      /* a kernel refused a malformed device-side table */
 int ctgb_device_status(int32_t *out, int32_t clear);
+/* Self-test of the bounded device waits every TMA/mbarrier kernel uses: one
+ * warp waits, with a limit of `polls` polls (1 .. 2^20), on an mbarrier that
+ * nothing arrives at; the wait runs out, sets CTGB_DEVERR_TIMEOUT in the
+ * device status word, and the kernel returns (the context stays usable).
+ * Stream-ordered.  No reference counterpart. */
+int ctgb_selftest_bounded_wait(int32_t polls, void *stream);
 /* The calling thread's last error message; replaces the reference's
  * ErrorDescription printouts followed by sys.exit()
  * (Reconstruction_numba.py:36-52). */

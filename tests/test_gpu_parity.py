@@ -171,6 +171,31 @@ def test_bad_inputs_raise(cuda):
         P.forward(torch.rand((3, 3, 3), device=cuda))
 
 
+def test_bounded_wait_runs_out_into_the_status_word(cuda):
+    """A bounded device wait that nothing satisfies (the self-test kernel's
+    mbarrier gets no arrival) gives up after its poll limit, sets
+    CTGB_DEVERR_TIMEOUT in the device status word and returns; the context
+    stays usable (a projection afterwards matches the oracle) and the status
+    clears."""
+    import ctypes
+    from ctreconstruction_gb300 import _lib
+    st = ctypes.c_int32(0)
+    _lib.call("ctgb_device_status", ctypes.byref(st), 1)            # start clean
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.call("ctgb_selftest_bounded_wait", 1000, stream)
+    _lib.call("ctgb_device_status", ctypes.byref(st), 1)
+    assert st.value & 1, st.value                                    # CTGB_DEVERR_TIMEOUT
+    _lib.call("ctgb_device_status", ctypes.byref(st), 0)
+    assert st.value == 0
+    p = GEOMS["tma_cone"]
+    g = OracleGeometry(p)
+    P = Projector(p)
+    x = np.random.default_rng(3).random((g.nz, g.ny, g.nx), dtype=np.float32)
+    assert rel_err(P.forward(_t(x, cuda)).cpu().numpy(), g.forward(x)) < RTOL
+    _lib.call("ctgb_device_status", ctypes.byref(st), 0)
+    assert st.value == 0
+
+
 def test_device_status_clean_after_runs(cuda):
     """No kernel reported a wait timeout or bounds problem."""
     import ctypes
