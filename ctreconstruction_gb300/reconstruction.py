@@ -136,7 +136,10 @@ class Reconstruction:
     def _forward_pinned(self, src):
         P = self.projector
         compute, copy = self._streams()
-        vol = _to_device(src, P.device)
+        if tuple(src.shape) != tuple(P.volume_shape):
+            raise ValueError("image must have shape %s, got %s" % (tuple(P.volume_shape), tuple(src.shape)))
+        vol = self._device_buffer("vol", P.volume_shape)
+        vol.copy_(src, non_blocking=True)
         xzy = P.transpose(vol)
         shape = P.proj_shape()
         dev = self._device_buffer("proj", shape)
@@ -158,7 +161,7 @@ class Reconstruction:
         if tuple(src.shape) != tuple(shape):
             raise ValueError("proj must have shape %s, got %s" % (shape, tuple(src.shape)))
         q = self._device_buffer("proj_in", shape)
-        vol = torch.empty(P.volume_shape, dtype=torch.float32, device=P.device)
+        vol = self._device_buffer("vol", P.volume_shape)
         # Symmetric orbits: each chunk is a range of base views, whose nc
         # slabs (one per 1/nc turn) are copied before its launch.
         nc = P.orbit_size()
