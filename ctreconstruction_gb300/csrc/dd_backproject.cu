@@ -458,16 +458,18 @@ constexpr int kWkTX = 4, kWkTY = 32, kWkThreads = kWkTX * kWkTY;   // 4 x 32 col
 template <int NC> struct WalkShape;
 template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8; };
 template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8; };
-// Quarter-turn orbits: at 512^3 / 720 views Z = 12 with 7 CTAs per SM took
-// 140.3 ms (Z = 8 at 8 CTAs 152.2, Z = 16 at 6 CTAs 146.8, Z = 24 at 4
-// 146.7, Z = 32 at 3 181.0; the voxel loop unrolled by 2 or 4: 157, 159 at
-// Z = 16): a longer chunk shares each (column, view) set-up between more
+// Quarter-turn orbits: at 512^3 / 720 views, with the columns paired into
+// f32x2 lanes and 32-bit view offsets, Z = 16 at 6 CTAs per SM took 128.4 ms
+// (Z = 12 at 7: 140.8, at 8: 137.1; Z = 20 at 5: 135.7).  With scalar
+// columns: Z = 12 at 7 140.3 ms (Z = 8 at 8 152.2, Z = 16 at 6 146.8, Z = 24
+// at 4 146.7, Z = 32 at 3 181.0; the voxel loop unrolled by 2 or 4: 157, 159
+// at Z = 16): a longer chunk shares each (column, view) set-up between more
 // voxels, fewer resident warps hide less of the row loads' latency.
 #ifndef CTGB_WALK_Z4
-#define CTGB_WALK_Z4 12
+#define CTGB_WALK_Z4 16
 #endif
 #ifndef CTGB_WALK_B4
-#define CTGB_WALK_B4 7
+#define CTGB_WALK_B4 6
 #endif
 template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = CTGB_WALK_B4; };
 
@@ -544,7 +546,90 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
         const float dh = p.y - curf;
         float *__restrict__ sa = sacc + j * NC * kWkThreads;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) sa[k * kWkThreads] += (fmaf(Rc[k], dh, Gc[k]) - glo[k]) * rw;
+        for (int k = 0; k < NC; ++k) sa[k] += (fmaf(Rc[k], dh, Gc[k]) - glo[k]) * rw;
+    }
+}
+
+// The same walk for NC = 2 or 4 columns, the columns' values paired into
+// float2 lanes (columns 2p and 2p + 1) so that the row sums, the running G
+// and the voxel ends take one packed f32x2 operation per pair; the voxel's
+// NC sums are adjacent in shared memory (one 8- or 16-byte access).
+template <int NC, int Z, int NT, bool CLAMP>
+__device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj, const int (&vb)[NC], int nu, int nv,
+                                                 const float (&ov)[4], bool lin, float lo0, float hi0, float dlo,
+                                                 float dhi, float zfirst, float dzs, float hz, float Sz, float imin,
+                                                 float imax, float Mv, float Av, float *sacc) {
+    constexpr int NP = NC / 2;
+    auto pos = [&](int j) {
+        if (lin) return __ffma2_rn(make_float2((float)j, (float)j), make_float2(dlo, dhi), make_float2(lo0, hi0));
+        float a, b;
+        v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &a, &b);
+        return make_float2(a, b);
+    };
+    auto rows = [&](int r, int roff, float2 (&out)[NP]) {
+        const bool in = !CLAMP || (unsigned)r < (unsigned)nv;
+        const int off = in ? roff : 0;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            const float *__restrict__ a = proj + (vb[2 * q] + off);
+            const float *__restrict__ b = proj + (vb[2 * q + 1] + off);
+            float2 t2 = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int t = 0; t < NT; ++t)
+                t2 = __ffma2_rn(make_float2(ov[t], ov[t]), make_float2(__ldg(a + t), __ldg(b + t)), t2);
+            out[q] = in ? t2 : make_float2(0.0f, 0.0f);
+        }
+    };
+    const float2 p0 = pos(0);
+    float curf;
+    int cur = floor_split(p0.x, &curf);
+    int roff = cur * nu;
+    float2 Gc[NP], Rc[NP], Rp[NP], Rn[NP];
+    rows(cur, roff, Rc);
+    rows(cur + 1, roff + nu, Rn);
+#pragma unroll
+    for (int q = 0; q < NP; ++q) { Gc[q] = make_float2(0.0f, 0.0f); Rp[q] = make_float2(0.0f, 0.0f); }
+    auto advance = [&]() {
+        cur += 1;
+        roff += nu;
+        curf += 1.0f;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+            Gc[q] = __fadd2_rn(Gc[q], Rc[q]);
+            Rp[q] = Rc[q];
+            Rc[q] = Rn[q];
+        }
+        rows(cur + 1, roff + nu, Rn);
+    };
+#pragma unroll (kWalkUnroll)
+    for (int j = 0; j < Z; ++j) {
+        const float2 p = pos(j);
+        const float rw = fast_rcp(p.y - p.x);
+        const float dl = p.x - curf;
+        const float2 dl2 = make_float2(dl, dl);
+        float2 glo[NP];
+        const bool above = dl >= 0.0f;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) glo[q] = __ffma2_rn(above ? Rc[q] : Rp[q], dl2, Gc[q]);
+#pragma unroll 1
+        for (int a = 0; a < 3 && p.y - curf >= 1.0f; ++a) advance();
+        const float dh = p.y - curf;
+        const float2 dh2 = make_float2(dh, dh), rw2 = make_float2(rw, rw);
+        float2 v[NP];
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+            v[q] = __fmul2_rn(__fadd2_rn(__ffma2_rn(Rc[q], dh2, Gc[q]), make_float2(-glo[q].x, -glo[q].y)), rw2);
+        float *__restrict__ sa = sacc + j * NC * kWkThreads;
+        if (NC == 4) {
+            float4 *a4 = reinterpret_cast<float4 *>(sa);
+            float4 a = *a4;
+            const float2 lo2 = __fadd2_rn(make_float2(a.x, a.y), v[0]);
+            const float2 hi2 = __fadd2_rn(make_float2(a.z, a.w), v[NP - 1]);
+            *a4 = make_float4(lo2.x, lo2.y, hi2.x, hi2.y);
+        } else {
+            float2 *a2 = reinterpret_cast<float2 *>(sa);
+            *a2 = __fadd2_rn(*a2, v[0]);
+        }
     }
 }
 
@@ -559,11 +644,14 @@ __global__ void __launch_bounds__(kWkThreads, WalkShape<NC>::MINB)
 bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, float *__restrict__ vol, int view0,
                    int nviews, float scale, int accumulate) {
     constexpr int Z = WalkShape<NC>::Z;
-    __shared__ float sacc_all[Z * NC * kWkThreads];
+    // voxel j of orbit column k at sacc[j * NC * kWkThreads + k] (this thread's NC sums adjacent)
+    __shared__ __align__(16) float sacc_all[Z * NC * kWkThreads];
     const int tid = threadIdx.y * kWkTX + threadIdx.x;
-    float *sacc = sacc_all + tid;
+    float *sacc = sacc_all + tid * NC;
 #pragma unroll 1
-    for (int i = 0; i < Z * NC; ++i) sacc[i * kWkThreads] = 0.0f;
+    for (int j = 0; j < Z; ++j)
+#pragma unroll
+        for (int k = 0; k < NC; ++k) sacc[j * NC * kWkThreads + k] = 0.0f;
     const TableHeader &h = header(T);
     const int nu = h.nu, nv = h.nv, nz = h.nz, nxh = h.nx, nyh = h.ny;
     const int ix = blockIdx.x * kWkTX + threadIdx.x;
@@ -685,10 +773,21 @@ bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, 
         const bool lin = __all_sync(0xffffffffu, linear || !ok);
         if (ok) {
             const float *vb[NC];
+            int vo[NC];   // element offsets of the views' column lbase (< 2^31, checked by the host)
 #pragma unroll
-            for (int k = 0; k < NC; ++k) vb[k] = proj + (long long)pv[k] * vstride + lbase;
-#define CTGB_WALK(NTV, C) \
-    walk_rows<NC, Z, NTV, C>(vb, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, imax, Mv, Av, sacc)
+            for (int k = 0; k < NC; ++k) {
+                vb[k] = proj + (long long)pv[k] * vstride + lbase;
+                vo[k] = pv[k] * (int)vstride + lbase;
+            }
+#define CTGB_WALK(NTV, C)                                                                                      \
+    do {                                                                                                       \
+        if constexpr (NC == 1)                                                                                 \
+            walk_rows<NC, Z, NTV, C>(vb, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, imax, Mv, \
+                                     Av, sacc);                                                                \
+        else                                                                                                   \
+            walk_rows_packed<NC, Z, NTV, C>(proj, vo, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, \
+                                            imax, Mv, Av, sacc);                                               \
+    } while (0)
             if (!clamp) {
                 if (nt <= 2) CTGB_WALK(2, false);
                 else if (nt == 3) CTGB_WALK(3, false);
@@ -727,7 +826,7 @@ bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, 
                             part += __ldg(qrow + l) * span_weight<false>(us, l, ki[l], ki[l + 1], abs_du, eps);
                         sum += part * w1;
                     }
-                    sacc[(j * NC + k) * kWkThreads] += sum * Wd;
+                    sacc[j * NC * kWkThreads + k] += sum * Wd;
                 }
             }
         }
@@ -751,7 +850,7 @@ bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, 
             const int iz = z0 + j;
             if (iz < nz) {
                 float *dst = vol + ((long long)iz * nyh + cy) * nxh + cx;
-                const float b = sacc[(j * NC + k) * kWkThreads];
+                const float b = sacc[j * NC * kWkThreads + k];
                 *dst = accumulate ? __fadd_rn(*dst, b) : b;
             }
         }
@@ -1608,7 +1707,14 @@ static void launch_walk(bool curved, dim3 grid, cudaStream_t s, const float *T, 
         bp_fdk_walk_kernel<false, NC><<<grid, block, 0, s>>>(T, proj, vol, view0, nviews, scale, accumulate);
 }
 
+// The paired (2- and 4-column) walks address the projections with 32-bit
+// element offsets.
+static bool walk_offsets_fit(const ctgb_params *p) {
+    return (long long)p->nviews * p->nu * p->nv < (1LL << 31);
+}
+
 static int fdk_orbit(const ctgb_params *p) {
+    if (!walk_offsets_fit(p)) return 1;
     if (CTGB_WALK_NC >= 4 && fdk_fourfold(p)) return 4;
     if (CTGB_WALK_NC >= 2 && fdk_twofold(p)) return 2;
     return 1;
@@ -1679,11 +1785,12 @@ extern "C" int ctgb_backproject_fdk(const ctgb_params *p, const void *d_table, c
     if ((long long)p->nu * (p->nv + 2) >= (1LL << 31))
         return set_error(CTGB_ERR_SIZE, "ctgb_backproject_fdk: detector of %d x %d pixels too large", p->nu, p->nv);
     const bool full = view0 == 0 && nviews == p->nviews;
-    if (CTGB_WALK_NC >= 4 && full && fdk_fourfold(p)) {
+    const int nc = full ? fdk_orbit(p) : 1;
+    if (nc == 4) {
         const int hn = p->nx / 2;
         dim3 grid((hn + kWkTX - 1) / kWkTX, (hn + kWkTY - 1) / kWkTY, (p->nz + WalkShape<4>::Z - 1) / WalkShape<4>::Z);
         launch_walk<4>(p->curved, grid, s, T, d_proj, d_vol, 0, p->nviews / 4, scale, accumulate);
-    } else if (CTGB_WALK_NC >= 2 && full && fdk_twofold(p)) {
+    } else if (nc == 2) {
         dim3 grid((p->nx + kWkTX - 1) / kWkTX, (p->ny / 2 + kWkTY - 1) / kWkTY,
                   (p->nz + WalkShape<2>::Z - 1) / WalkShape<2>::Z);
         launch_walk<2>(p->curved, grid, s, T, d_proj, d_vol, 0, p->nviews / 2, scale, accumulate);
@@ -1739,7 +1846,7 @@ extern "C" int ctgb_backproject_fdk_ws(const ctgb_params *p, const void *d_table
     }
     // A full orbit with four-fold symmetry runs the row walk over the raw
     // projections (no workspace needed): faster than integrating them.
-    if (CTGB_WALK_NC >= 4 && view0 == 0 && nviews == p->nviews && fdk_fourfold(p))
+    if (view0 == 0 && nviews == p->nviews && fdk_orbit(p) == 4)
         return ctgb_backproject_fdk(p, d_table, d_proj, d_vol, view0, nviews, scale, accumulate, stream);
     const size_t per_view = (size_t)(p->nv + 1) * (size_t)p->nu * sizeof(float2);
     const int chunk = (int)(workspace_bytes / per_view);
