@@ -541,8 +541,13 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
         float glo[NC];
 #pragma unroll
         for (int k = 0; k < NC; ++k) glo[k] = fmaf(dl >= 0.0f ? Rc[k] : Rp[k], dl, Gc[k]);
+        // at most three rows per voxel; the first step outside the loop
+        // (122.6 against 128.5 ms at 512^3 / 720 views)
+        if (p.y - curf >= 1.0f) {
+            advance();
 #pragma unroll 1
-        for (int a = 0; a < 3 && p.y - curf >= 1.0f; ++a) advance();
+            for (int a = 0; a < 2 && p.y - curf >= 1.0f; ++a) advance();
+        }
         const float dh = p.y - curf;
         float *__restrict__ sa = sacc + j * NC * kWkThreads;
 #pragma unroll
@@ -611,8 +616,13 @@ __device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj,
         const bool above = dl >= 0.0f;
 #pragma unroll
         for (int q = 0; q < NP; ++q) glo[q] = __ffma2_rn(above ? Rc[q] : Rp[q], dl2, Gc[q]);
+        // at most three rows per voxel; the first step outside the loop
+        // (122.6 against 128.5 ms at 512^3 / 720 views)
+        if (p.y - curf >= 1.0f) {
+            advance();
 #pragma unroll 1
-        for (int a = 0; a < 3 && p.y - curf >= 1.0f; ++a) advance();
+            for (int a = 0; a < 2 && p.y - curf >= 1.0f; ++a) advance();
+        }
         const float dh = p.y - curf;
         const float2 dh2 = make_float2(dh, dh), rw2 = make_float2(rw, rw);
         float2 v[NP];
