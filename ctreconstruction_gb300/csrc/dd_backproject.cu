@@ -481,8 +481,8 @@ template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = 
 // rows per voxel and overlap their predecessor by under one row, so three row
 // steps per voxel always suffice.  (With the source at +y and the detector
 // at -y, as in every reference script, rows grow with the voxel index: row
-// coordinates run opposite to z on both axes.)  Voxel j of view k adds into
-// sacc[(j * NC + k) * kWkThreads].
+// coordinates run opposite to z on both axes.)  Voxel j of column k adds
+// into sacc[j * NC * kWkThreads + k] (sacc: this thread's slots).
 #ifndef CTGB_WALK_UNROLL
 #define CTGB_WALK_UNROLL 1
 #endif
@@ -559,14 +559,14 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
 // float2 lanes (columns 2p and 2p + 1) so that the row sums, the running G
 // and the voxel ends take one packed f32x2 operation per pair; the voxel's
 // NC sums are adjacent in shared memory (one 8- or 16-byte access).
-template <int NC, int Z, int NT, bool CLAMP>
+template <int NC, int Z, int NT, bool CLAMP, bool LIN>
 __device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj, const int (&vb)[NC], int nu, int nv,
-                                                 const float (&ov)[4], bool lin, float lo0, float hi0, float dlo,
+                                                 const float (&ov)[4], float lo0, float hi0, float dlo,
                                                  float dhi, float zfirst, float dzs, float hz, float Sz, float imin,
                                                  float imax, float Mv, float Av, float *sacc) {
     constexpr int NP = NC / 2;
     auto pos = [&](int j) {
-        if (lin) return __ffma2_rn(make_float2((float)j, (float)j), make_float2(dlo, dhi), make_float2(lo0, hi0));
+        if (LIN) return __ffma2_rn(make_float2((float)j, (float)j), make_float2(dlo, dhi), make_float2(lo0, hi0));
         float a, b;
         v_footprint(zfirst + (float)j * dzs, hz, Sz, imin, imax, Mv, Av, &a, &b);
         return make_float2(a, b);
@@ -794,9 +794,12 @@ bp_fdk_walk_kernel(const float *__restrict__ T, const float *__restrict__ proj, 
         if constexpr (NC == 1)                                                                                 \
             walk_rows<NC, Z, NTV, C>(vb, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, imax, Mv, \
                                      Av, sacc);                                                                \
+        else if (lin)                                                                                          \
+            walk_rows_packed<NC, Z, NTV, C, true>(proj, vo, nu, nv, ov, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz,  \
+                                                  imin, imax, Mv, Av, sacc);                                   \
         else                                                                                                   \
-            walk_rows_packed<NC, Z, NTV, C>(proj, vo, nu, nv, ov, lin, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, imin, \
-                                            imax, Mv, Av, sacc);                                               \
+            walk_rows_packed<NC, Z, NTV, C, false>(proj, vo, nu, nv, ov, lo0, hi0, dlo, dhi, zfirst, dzs, hz, Sz, \
+                                                   imin, imax, Mv, Av, sacc);                                  \
     } while (0)
             if (!clamp) {
                 if (nt <= 2) CTGB_WALK(2, false);
