@@ -432,11 +432,13 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
 // column, so detector row r contributes one value R(r) = sum_t w_t p[r][lbase
 // + t].  The column's voxel footprints [lo, hi] (row units) move
 // monotonically with z and consecutive ones overlap by less than a row, so
-// the thread walks up the rows once per (column, view), keeping
-// G(r) = sum_{r' < r} R(r') and the R of the rows at the walk front in
-// registers: a voxel's footprint integral is G(hi) - G(lo) with
-// G(v) = G(floor v) + R(floor v) frac(v), divided by the footprint's width —
-// the reference's weight_calculator1 sum over rows.  Each detector row under
+// the thread walks up the rows once per (column, view), keeping the R of the
+// rows at the walk front in registers.  With G(r) = sum_{r' < r} R(r') and
+// G(v) = G(floor v) + R(floor v) frac(v), a voxel's footprint integral
+// G(hi) - G(lo), divided by the footprint's width, is the reference's
+// weight_calculator1 sum over rows; the walk forms it locally, as the rows
+// the voxel crosses plus the partial rows at its two ends, so no running sum
+// (and no cancellation between two large ones) is involved.  Each detector row under
 // the column is read once per view (NT 4-byte loads) instead of two 8-byte
 // running-sum lookups per tap and voxel, and no integrated copy of the
 // projections is made.
@@ -459,17 +461,17 @@ template <int NC> struct WalkShape;
 template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8; };
 template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8; };
 // Quarter-turn orbits: at 512^3 / 720 views, with the columns paired into
-// f32x2 lanes and 32-bit view offsets, Z = 16 at 6 CTAs per SM took 128.4 ms
-// (Z = 12 at 7: 140.8, at 8: 137.1; Z = 20 at 5: 135.7).  With scalar
-// columns: Z = 12 at 7 140.3 ms (Z = 8 at 8 152.2, Z = 16 at 6 146.8, Z = 24
-// at 4 146.7, Z = 32 at 3 181.0; the voxel loop unrolled by 2 or 4: 157, 159
-// at Z = 16): a longer chunk shares each (column, view) set-up between more
-// voxels, fewer resident warps hide less of the row loads' latency.
+// f32x2 lanes, the local voxel integrals and the row steps written out,
+// Z = 14 at 7 CTAs per SM takes 106.9 ms (Z = 16 at 6: 111.2; Z = 12 at 8:
+// 107.6; Z = 13 or 15 at 7: 107.8, 107.4; Z = 20 at 5: 120.3).  A longer
+// chunk shares each (column, view) set-up between more voxels, fewer
+// resident warps hide less of the row loads' latency.  (The running-sum walk
+// with a counted step loop: Z = 16 at 6 121.0 ms.)
 #ifndef CTGB_WALK_Z4
-#define CTGB_WALK_Z4 16
+#define CTGB_WALK_Z4 14
 #endif
 #ifndef CTGB_WALK_B4
-#define CTGB_WALK_B4 6
+#define CTGB_WALK_B4 7
 #endif
 template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = CTGB_WALK_B4; };
 
@@ -515,19 +517,20 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
     float curf;
     int cur = floor_split(p0.x, &curf);
     int roff = cur * nu;
-    float Gc[NC], Rc[NC], Rp[NC], Rn[NC];   // G(cur), R(cur), R(cur - 1), R(cur + 1)
+    // R(cur), R(cur + 1), D = R(cur) - R(cur - 1), and the voxel's integral so far
+    float Rc[NC], Rn[NC], D[NC], A[NC];
     rows(cur, roff, Rc);
     rows(cur + 1, roff + nu, Rn);
 #pragma unroll
-    for (int k = 0; k < NC; ++k) { Gc[k] = 0.0f; Rp[k] = 0.0f; }
+    for (int k = 0; k < NC; ++k) D[k] = 0.0f;
     auto advance = [&]() {
         cur += 1;
         roff += nu;
         curf += 1.0f;
 #pragma unroll
         for (int k = 0; k < NC; ++k) {
-            Gc[k] += Rc[k];
-            Rp[k] = Rc[k];
+            A[k] += Rc[k];
+            D[k] = Rn[k] - Rc[k];
             Rc[k] = Rn[k];
         }
         rows(cur + 1, roff + nu, Rn);
@@ -536,22 +539,24 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
     for (int j = 0; j < Z; ++j) {
         const float2 p = pos(j);
         const float rw = fast_rcp(p.y - p.x);
-        // lo lies in row cur or cur - 1; G(lo) = G(cur) + R(row) (lo - cur) either way
-        const float dl = p.x - curf;
-        float glo[NC];
+        // lo lies in row cur or cur - 1: G(lo) - G(cur) = R(cur) dl - D m, with
+        // dl = lo - cur and m = max(-dl, 0) (zero in row cur)
+        const float dl = p.x - curf, m = __saturatef(-dl);
 #pragma unroll
-        for (int k = 0; k < NC; ++k) glo[k] = fmaf(dl >= 0.0f ? Rc[k] : Rp[k], dl, Gc[k]);
-        // at most three rows per voxel; the first step outside the loop
-        // (122.6 against 128.5 ms at 512^3 / 720 views)
+        for (int k = 0; k < NC; ++k) A[k] = fmaf(Rc[k], -dl, D[k] * -m);
+        // at most three rows per voxel, the steps written out (111.2 against
+        // 115.5 ms with a counted loop for the second and third)
         if (p.y - curf >= 1.0f) {
             advance();
-#pragma unroll 1
-            for (int a = 0; a < 2 && p.y - curf >= 1.0f; ++a) advance();
+            if (p.y - curf >= 1.0f) {
+                advance();
+                if (p.y - curf >= 1.0f) advance();
+            }
         }
         const float dh = p.y - curf;
         float *__restrict__ sa = sacc + j * NC * kWkThreads;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) sa[k] += (fmaf(Rc[k], dh, Gc[k]) - glo[k]) * rw;
+        for (int k = 0; k < NC; ++k) sa[k] += fmaf(Rc[k], dh, A[k]) * rw;
     }
 }
 
@@ -589,19 +594,19 @@ __device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj,
     float curf;
     int cur = floor_split(p0.x, &curf);
     int roff = cur * nu;
-    float2 Gc[NP], Rc[NP], Rp[NP], Rn[NP];
+    float2 Rc[NP], Rn[NP], D[NP], A[NP];   // as in walk_rows, column pairs
     rows(cur, roff, Rc);
     rows(cur + 1, roff + nu, Rn);
 #pragma unroll
-    for (int q = 0; q < NP; ++q) { Gc[q] = make_float2(0.0f, 0.0f); Rp[q] = make_float2(0.0f, 0.0f); }
+    for (int q = 0; q < NP; ++q) D[q] = make_float2(0.0f, 0.0f);
     auto advance = [&]() {
         cur += 1;
         roff += nu;
         curf += 1.0f;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
-            Gc[q] = __fadd2_rn(Gc[q], Rc[q]);
-            Rp[q] = Rc[q];
+            A[q] = __fadd2_rn(A[q], Rc[q]);
+            D[q] = __fadd2_rn(Rn[q], make_float2(-Rc[q].x, -Rc[q].y));
             Rc[q] = Rn[q];
         }
         rows(cur + 1, roff + nu, Rn);
@@ -610,25 +615,22 @@ __device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj,
     for (int j = 0; j < Z; ++j) {
         const float2 p = pos(j);
         const float rw = fast_rcp(p.y - p.x);
-        const float dl = p.x - curf;
-        const float2 dl2 = make_float2(dl, dl);
-        float2 glo[NP];
-        const bool above = dl >= 0.0f;
+        const float dl = p.x - curf, m = __saturatef(-dl);
+        const float2 ndl2 = make_float2(-dl, -dl), nm2 = make_float2(-m, -m);
 #pragma unroll
-        for (int q = 0; q < NP; ++q) glo[q] = __ffma2_rn(above ? Rc[q] : Rp[q], dl2, Gc[q]);
-        // at most three rows per voxel; the first step outside the loop
-        // (122.6 against 128.5 ms at 512^3 / 720 views)
+        for (int q = 0; q < NP; ++q) A[q] = __ffma2_rn(Rc[q], ndl2, __fmul2_rn(D[q], nm2));
         if (p.y - curf >= 1.0f) {
             advance();
-#pragma unroll 1
-            for (int a = 0; a < 2 && p.y - curf >= 1.0f; ++a) advance();
+            if (p.y - curf >= 1.0f) {
+                advance();
+                if (p.y - curf >= 1.0f) advance();
+            }
         }
         const float dh = p.y - curf;
         const float2 dh2 = make_float2(dh, dh), rw2 = make_float2(rw, rw);
         float2 v[NP];
 #pragma unroll
-        for (int q = 0; q < NP; ++q)
-            v[q] = __fmul2_rn(__fadd2_rn(__ffma2_rn(Rc[q], dh2, Gc[q]), make_float2(-glo[q].x, -glo[q].y)), rw2);
+        for (int q = 0; q < NP; ++q) v[q] = __fmul2_rn(__ffma2_rn(Rc[q], dh2, A[q]), rw2);
         float *__restrict__ sa = sacc + j * NC * kWkThreads;
         if (NC == 4) {
             float4 *a4 = reinterpret_cast<float4 *>(sa);
