@@ -52,17 +52,17 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary
-    (a line 'traffic_bytes_per_launch: <N>' in profiles/<kernel>*.md), or None."""
+def profiled_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` on `workload` from the committed ncu
+    summary profiles/<kernel>_<workload>.md (a line 'traffic_bytes_per_launch:
+    <N>'), or None when that workload's launches were not captured."""
     d = os.path.join(REPO, "profiles")
-    if not os.path.isdir(d):
-        return None
-    for f in sorted(os.listdir(d)):
-        if f.startswith(kernel) and f.endswith((".md", ".txt")):
-            with open(os.path.join(d, f)) as fh:
-                lines = fh.readlines()
-            for line in lines:
+    for ext in (".md", ".txt"):
+        path = os.path.join(d, "%s_%s%s" % (kernel, workload, ext))
+        if not os.path.exists(path):
+            continue
+        with open(path) as fh:
+            for line in fh:
                 if line.strip().startswith("traffic_bytes_per_launch:"):
                     try:
                         return float(line.split(":", 1)[1].split()[0])
@@ -278,7 +278,7 @@ def run_ours(args):
     achieved = alg_bytes / (per_launch[dom] / 1e3) / 1e9
     kname = {"forward": "dd_forward_tma_kernel", "backproject_fdk": "bp_fdk_walk_kernel"}[dom]
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(kname),
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(kname, "dd_pair" if not args.small else "small"),
                 "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": per_launch[dom],
                 "per_kernel_frac": {k: 4.0 * vv / (kern[k] / 1e3) / 1e9 / peak for k in ("forward", "backproject_fdk")}}
 
@@ -417,14 +417,15 @@ def _lib_call(name, *args):
     _lib.call(name, *conv, first.numel(), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
 
-def hbm_roofline(kernel, ms_per_launch, alg_bytes, what):
+def hbm_roofline(kernel, ms_per_launch, alg_bytes, what, workload):
     """roofline object for an HBM-bound kernel: algorithmic bytes per launch
     (`what` says how they are counted) over its CUDA-event time per launch,
-    against the measured copy bandwidth."""
+    against the measured copy bandwidth; DRAM traffic from the workload's own
+    ncu summary where one is committed."""
     peak, kind = measured_peaks()
     achieved = alg_bytes / (ms_per_launch / 1e3) / 1e9
     return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": kind, "traffic": profiled_traffic(kernel),
+            "frac": achieved / peak, "peak_source": kind, "traffic": profiled_traffic(kernel, workload),
             "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": ms_per_launch, "bytes_model": what}
 
 
@@ -490,9 +491,10 @@ def run_fdk128(args):
     rmse = float(torch.sqrt(torch.mean((out - ph)[inner] ** 2)))
     dom = max(("filter", "backproject"), key=lambda k: per[k])
     if dom == "backproject":
-        roof = hbm_roofline("bp_fdk_walk_kernel", per["backproject"], 4.0 * vv, "4 B per voxel-view")
+        roof = hbm_roofline("bp_fdk_walk_kernel", per["backproject"], 4.0 * vv, "4 B per voxel-view", "fdk128")
     else:
-        roof = hbm_roofline("fdk_filter_kernel", per["filter"], 8.0 * 360 * 256 * 192, "8 B per detector pixel")
+        roof = hbm_roofline("fdk_filter_kernel", per["filter"], 8.0 * 360 * 256 * 192, "8 B per detector pixel",
+                            "fdk128")
     roof["per_stage_ms"] = per
     cpu = None
     if not args.no_cpu:
@@ -587,7 +589,7 @@ def run_fan_batch(args):
     pv = sum(n * n for n in sizes) * nviews
     # Dominant kernel: the persistent backprojection (one launch per batch).
     bp_ms = max(out["line"]["per_stage_ms"]["backproject"], out["arc"]["per_stage_ms"]["backproject"])
-    roof = hbm_roofline("fan_bp_kernel", bp_ms, 4.0 * pv, "4 B per pixel-view")
+    roof = hbm_roofline("fan_bp_kernel", bp_ms, 4.0 * pv, "4 B per pixel-view", "fan_batch")
     cpu = None
     if not args.no_cpu:
         # FanBeam.py's own reconstruction restated in FP64 NumPy
@@ -689,7 +691,7 @@ def run_iter(args):
     roof = hbm_roofline({"forward": "dd_forward_tma_kernel",
                          "backproject_matched": "bp_matched_integ_kernel"}[dom], per[dom], 4.0 * vv_sub,
                         "4 B per voxel-view (one 9-view subset of the 384^3 scan; the backprojection's time "
-                        "includes its integration pass)")
+                        "includes its integration pass)", "iter")
     roof["per_stage_ms_384cube_subset"] = per
     del solver
     cpu = None
@@ -769,7 +771,7 @@ def _asd_roofline_cpu(P, x, args, niter_label="outer iteration"):
     share = {"forward": 5 * per["forward"], "backproject": 5 * per["backproject"], "tv20": per["tv20"]}
     dom = max(share, key=share.get)
     ms_l, by, kname, what = cand[dom]
-    roof = hbm_roofline(kname, ms_l, by, what)
+    roof = hbm_roofline(kname, ms_l, by, what, "asd256")
     roof["per_stage_ms"] = per
     cpu = None
     if not args.no_cpu:
@@ -959,7 +961,7 @@ def run_rows(args):
     nfwd = Projector(dict(base, DetectorShape='Curved'), device=dev).forward_launches()
     roof = hbm_roofline({"forward": "dd_forward_tma_kernel", "backproject": "bp_fdk_walk_kernel"}[dom],
                         per[dom] / (nfwd if dom == "forward" else 1), 4.0 * vv / (nfwd if dom == "forward" else 1),
-                        "4 B per voxel-view, curved detector")
+                        "4 B per voxel-view, curved detector", "rows")
     cpu = None
     if not args.no_cpu:
         # Curved detectors run only in the reference's numba flavour (its
