@@ -168,8 +168,8 @@ __global__ void transpose_xy_batch_kernel(const TransJob *__restrict__ jobs, int
 //     two weight denominators become K_pixel / q^2 — one factor per slice;
 //   * h(m) = sum_k P[m][k] * overlap_x(k) for the lane's column (2-4 taps,
 //     overlaps in voxel units), and the row integral over [z'_j, z'_j+1] is
-//     sum of whole cells + e(z'_j+1) - e(z'_j) with e(z) = h(floor z) * frac(z),
-//     so consecutive rows share their boundary term.
+//     h at each end cell times its covered part plus any whole cell between;
+//     consecutive rows share their boundary cell's h.
 // Slices whose window exceeds the patch, or whose footprint is wider than 4
 // voxels, are integrated cell by cell from global memory (compact, rare path).
 constexpr int kTU = 32, kBoxX = 64, kBoxZ = 8, kPX = kBoxX;
@@ -229,8 +229,7 @@ struct PatchCells {
 // cell in the middle); rows never cover four (checked per slice by the
 // caller).  No data-dependent branches.  Chain a is the .x and chain b the
 // .y of float2 pairs, so the boundary positions, floors, fractions, cell
-// values, end terms and row sums of both chains take one packed f32x2
-// operation each (147.9 -> 137.4 ms per 512^3 / 720-view forward against
+// values and row sums of both chains take one packed f32x2 operation each (147.9 -> 137.4 ms per 512^3 / 720-view forward against
 // the scalar pair); acc2[j] holds rows j and N + j.  Boundary j of the tile
 // sits at local z f + j * sg (the frame of row_frame; cells are local too,
 // PatchCells adds the frame's integer part).
@@ -256,11 +255,17 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, float f, fl
         f = __fadd2_rn(t, mag);                                     // floor as float
         fr = __ffma2_rn(f, neg1, z);                                // z - floor
     };
+    // Row [z0, z1] with cells m0 = floor z0 and m1 = floor z1 = m0 + d:
+    // h1 (z1 - m1) + h0 (m1 - z0) for d <= 1 (for d = 0 both cells are m0),
+    // plus (hm - h0) for a three-cell row (d = 2, only with MID), which turns
+    // h0's share into h0 (m0 + 1 - z0) and adds the whole middle cell hm.
+    // Carrying z0 instead of the end term h0 (z0 - m0) saves the per-row
+    // difference of end terms (117.0 -> 112.1 ms per 512^3 / 720-view forward
+    // with the three-cell case's selects as saturated factors).
     float2 z0 = __ffma2_rn(make_float2(0.0f, (float)N), sg2, f2), f0, fr0;
     int m0a, m0b;   // only addresses h0; later rows need only the float floors
     split(z0, m0a, m0b, f0, fr0);
     float2 h0 = H2(m0a, m0b);
-    float2 e0 = __fmul2_rn(h0, fr0);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
         const float2 z1 = __ffma2_rn(make_float2((float)(j + 1), (float)(N + j + 1)), sg2, f2);
@@ -268,25 +273,19 @@ __device__ __forceinline__ void sweep_rows2(const PatchCells<NT> &H, float f, fl
         float2 f1, fr1;
         split(z1, m1a, m1b, f1, fr1);
         const float2 h1 = H2(m1a, m1b);
-        const float2 e1 = __fmul2_rn(h1, fr1);
-        // Cells the row crosses: d = floor(z1) - floor(z0), 0 or 1 (0, 1 or 2
-        // with MID).  Without MID the whole cell h0 enters as h0 * d, an exact
-        // product, so the row is the sum a select would give in one packed FMA
-        // (136.0 -> 132.5 ms per 512^3 / 720-view forward with the integer
-        // compares and selects).  With MID, d selects h0 and the middle cell.
-        const float2 d = __ffma2_rn(f0, neg1, f1);
-        float2 r = __ffma2_rn(e0, neg1, e1);
+        float2 r = __ffma2_rn(h1, fr1, __fmul2_rn(h0, __fadd2_rn(f1, make_float2(-z0.x, -z0.y))));
         if (MID) {
             // the middle cell of a three-cell row is m1 - 1 (read for every
-            // row; the window's one-cell margin keeps it inside the patch)
+            // row; the window's one-cell margin keeps it inside the patch);
+            // max(d - 1, 0) is 1 for d = 2 and 0 otherwise, so (hm - h0)
+            // enters only there
+            const float2 d = __ffma2_rn(f0, neg1, f1);
             const float2 hm = H2(m1a - 1, m1b - 1);
-            r = __fadd2_rn(r, make_float2(d.x > 0.0f ? h0.x : 0.0f, d.y > 0.0f ? h0.y : 0.0f));
-            r = __fadd2_rn(r, make_float2(d.x > 1.0f ? hm.x : 0.0f, d.y > 1.0f ? hm.y : 0.0f));
-        } else {
-            r = __ffma2_rn(h0, d, r);
+            r = __ffma2_rn(__fadd2_rn(hm, make_float2(-h0.x, -h0.y)),
+                           make_float2(__saturatef(d.x - 1.0f), __saturatef(d.y - 1.0f)), r);
         }
         acc2[j] = __ffma2_rn(r, g2, acc2[j]);
-        h0 = h1; e0 = e1; f0 = f1;
+        h0 = h1; z0 = z1; f0 = f1;
     }
 }
 
