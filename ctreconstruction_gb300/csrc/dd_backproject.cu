@@ -1079,6 +1079,48 @@ bp_matched_sweep_kernel(const float *__restrict__ T, const float *__restrict__ p
 // instead of dividing per voxel column (the search was most of its time).
 __host__ __device__ __forceinline__ int matched_tab_stride(int nu) { return 2 * nu + 2; }
 
+// The forward's per-pixel factor K = base * sqrt(1 + t2^2) / rowspan of
+// column c of view V (dd_forward_tma_kernel's epilogue, same expressions),
+// with the view's column table entries written to tab on the way.
+struct MatchedColumn {
+    int axis;
+    float base, invD, Sz, rowspan;
+    const float *Pzr;
+    __device__ __forceinline__ float K(int r) const {
+        const float t2 = (Sz - Pzr[r]) * invD;
+        return base * sqrtf(1.0f + t2 * t2) / rowspan;
+    }
+};
+
+__device__ __forceinline__ MatchedColumn matched_column_setup(const TableHeader &h, const float *__restrict__ V,
+                                                              const ViewOffsets &vo, int c, float *__restrict__ tab) {
+    const int nu = h.nu;
+    MatchedColumn mc;
+    mc.axis = (int)V[VF_AXIS];
+    mc.base = 0.0f; mc.invD = 0.0f; mc.Sz = 0.0f; mc.rowspan = 1.0f;   // z-dominant: unused, finite
+    mc.Pzr = V + vo.pz;
+    if (mc.axis == 2) return mc;
+    const bool xd = mc.axis == 0;
+    const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX];
+    const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
+    const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
+    const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
+    const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
+    const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
+    const float inv_db = 1.0f / db;
+    const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
+    const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
+    mc.invD = 1.0f / (Sa - Pa[c]);
+    tab[c] = Eb0;
+    if (c == nu - 1) tab[nu] = Eb1;
+    tab[nu + 1 + c] = mc.invD;
+    const float t1 = (Sb - Pb[c]) * mc.invD;
+    mc.base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(mc.invD));
+    mc.rowspan = fabsf(V[VF_DB]);
+    mc.Sz = V[VF_SZ];
+    return mc;
+}
+
 // Column c of view vi (t = vi * nu + c) of the matched backprojector's
 // integration pass.
 __device__ __forceinline__ void matched_integrate_one(const float *__restrict__ T, const float *__restrict__ proj,
@@ -1089,43 +1131,66 @@ __device__ __forceinline__ void matched_integrate_one(const float *__restrict__ 
     const int vi = (int)(t / nu), c = (int)(t % nu);
     const ViewOffsets vo = view_offsets(nu, nv);
     const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
-    const int axis = (int)V[VF_AXIS];
     const float *__restrict__ q = proj + (long long)vi * nu * nv + c;
     float2 *__restrict__ o = out + (long long)vi * (nv + 1) * nu + c;
-    double run = 0.0;
-    if (axis == 2) {
+    const MatchedColumn mc = matched_column_setup(h, V, vo, c, tabs + (long long)vi * matched_tab_stride(nu));
+    if (mc.axis == 2) {
         for (int r = 0; r < nv; ++r) o[(long long)r * nu] = make_float2(0.0f, __ldg(q + (long long)r * nu));
         o[(long long)nv * nu] = make_float2(0.0f, 0.0f);
         return;
     }
-    const bool xd = axis == 0;
-    const float Sa = xd ? V[VF_SX] : V[VF_SY], Sb = xd ? V[VF_SY] : V[VF_SX], Sz = V[VF_SZ];
-    const float *__restrict__ Ba = V + (xd ? vo.bx : vo.by);
-    const float *__restrict__ Bb = V + (xd ? vo.by : vo.bx);
-    const float *__restrict__ Pa = V + (xd ? vo.px : vo.py);
-    const float *__restrict__ Pb = V + (xd ? vo.py : vo.px);
-    const float *__restrict__ Pzr = V + vo.pz;
-    const float da = xd ? h.dx : h.dy, db = xd ? h.dy : h.dx;
-    const float inv_db = 1.0f / db;
-    // The forward's per-pixel factor (dd_forward_tma_kernel epilogue), same expressions.
-    const float Eb0 = (Sb - Bb[c]) / (Sa - Ba[c]) * inv_db;
-    const float Eb1 = (Sb - Bb[c + 1]) / (Sa - Ba[c + 1]) * inv_db;
-    const float invD = 1.0f / (Sa - Pa[c]);
-    float *__restrict__ tab = tabs + (long long)vi * matched_tab_stride(nu);
-    tab[c] = Eb0;
-    if (c == nu - 1) tab[nu] = Eb1;
-    tab[nu + 1 + c] = invD;
-    const float t1 = (Sb - Pb[c]) * invD;
-    const float base = fabsf(da) * sqrtf(1.0f + t1 * t1) / (fabsf(Eb1 - Eb0) * fabsf(invD));
-    const float rowspan = fabsf(V[VF_DB]);
+    double run = 0.0;
     for (int r = 0; r < nv; ++r) {
-        const float t2 = (Sz - Pzr[r]) * invD;
-        const float K = base * sqrtf(1.0f + t2 * t2) / rowspan;
-        const float y = __ldg(q + (long long)r * nu) * K;
+        const float y = __ldg(q + (long long)r * nu) * mc.K(r);
         o[(long long)r * nu] = make_float2((float)run, y);
         run += y;
     }
     o[(long long)nv * nu] = make_float2((float)run, 0.0f);
+}
+
+// The integration pass for the quarter-turn orbit kernel: thread (w, c)
+// integrates column c of the four views w + k Q (Q = views / 4) and writes,
+// per row boundary r, one 32-byte cell {C_0..C_3, y'_0..y'_3} at
+// ((w * (nv + 1) + r) * nu + c), so the orbit kernel's four lookups of a row
+// boundary are two adjacent 16-byte loads.  Values and tables as
+// matched_integrate_one (the same expressions per view).
+__global__ void matched_integrate_orbit_kernel(const float *__restrict__ T, const float *__restrict__ proj,
+                                               float4 *__restrict__ out, float *__restrict__ tabs) {
+    const TableHeader &h = header(T);
+    const int nu = h.nu, nv = h.nv, Q = h.nviews / 4;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nu * Q) return;
+    const int w = (int)(t / nu), c = (int)(t % nu);
+    const ViewOffsets vo = view_offsets(nu, nv);
+    MatchedColumn mc[4];
+    const float *__restrict__ q[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int v = w + k * Q;
+        const float *__restrict__ V = T + h.off_views + (long long)v * h.view_stride;
+        mc[k] = matched_column_setup(h, V, vo, c, tabs + (long long)v * matched_tab_stride(nu));
+        q[k] = proj + (long long)v * nu * nv + c;
+    }
+    float4 *__restrict__ o = out + ((long long)w * (nv + 1) * nu + c) * 2;
+    double run[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int r = 0; r < nv; ++r) {
+        float y[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float raw = __ldg(q[k] + (long long)r * nu);
+            y[k] = mc[k].axis == 2 ? raw : raw * mc[k].K(r);
+        }
+        float4 *cell = o + (long long)r * nu * 2;
+        cell[0] = make_float4(mc[0].axis == 2 ? 0.0f : (float)run[0], mc[1].axis == 2 ? 0.0f : (float)run[1],
+                              mc[2].axis == 2 ? 0.0f : (float)run[2], mc[3].axis == 2 ? 0.0f : (float)run[3]);
+        cell[1] = make_float4(y[0], y[1], y[2], y[3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) run[k] += y[k];
+    }
+    float4 *cell = o + (long long)nv * nu * 2;
+    cell[0] = make_float4(mc[0].axis == 2 ? 0.0f : (float)run[0], mc[1].axis == 2 ? 0.0f : (float)run[1],
+                          mc[2].axis == 2 ? 0.0f : (float)run[2], mc[3].axis == 2 ? 0.0f : (float)run[3]);
+    cell[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 __global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
@@ -1320,12 +1385,17 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
 // owns the four columns of one rotation orbit (the grid covers a quadrant):
 // per set-up view it searches the candidate columns and places their rows
 // once, and per z boundary it computes the row coordinate, floor and
-// fraction once; only the four (C, y') lookups and sums are per column.
-// The integrated projections of every view are in the workspace (absolute
-// view index), so each column reads its own view v + k Q.
-// At 512^3 / 720 views: 12 voxels per chunk at 4 CTAs per SM (128
-// registers) 137.9 ms; 8 at 5 155.1, 8 at 6 260.1 and 12 at 5 288.0 (both
-// spill in the lookup loop), 16 at 4 296.8.
+// fraction once; only the four (C, y') values and sums are per column.
+// matched_integrate_orbit_kernel stores the four views w + t Q of a base
+// view w side by side per cell, so a boundary's four lookups are two
+// adjacent 16-byte loads and the columns' sums run in f32x2 pairs (183.5
+// -> 162.9 ms per call at 512^3 / 720 views against four 8-byte lookups in
+// four views' separate rows).  Set-up view w + s4 Q reads slot (s4 + k) & 3
+// for orbit column k, so the sums are kept in slot order and rotate by one
+// slot between quarter turns.
+// At 512^3 / 720 views (four 8-byte lookups): 12 voxels per chunk at 4 CTAs
+// per SM (128 registers) 137.9 ms for the kernel; 8 at 5 155.1, 8 at 6
+// 260.1 and 12 at 5 288.0 (both spill in the lookup loop), 16 at 4 296.8.
 #ifndef CTGB_MO_Z
 #define CTGB_MO_Z 12
 #endif
@@ -1335,12 +1405,12 @@ bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ 
 constexpr int kMoZ = CTGB_MO_Z;
 
 __global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MO_B)
-bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
+bp_matched_orbit_kernel(const float *__restrict__ T, const float4 *__restrict__ integ,
                         const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
                         float scale, int accumulate) {
     // Candidate columns of the current set-up view, per thread (registers
     // held them across the lookup loop at the cost of spills).
-    __shared__ float cand[7][kMC][kMiTX * kMiTY];   // column, 4 weights, tau, 1 / (tau dB)
+    __shared__ float cand[7][kMC][kMiTX * kMiTY];   // column, 4 weights (slot order), tau, 1 / (tau dB)
     const int tid = threadIdx.y * kMiTX + threadIdx.x;
     const TableHeader &h = header(T);
     const int n = h.nx, hn = n / 2, n1 = n - 1;
@@ -1353,24 +1423,43 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
     const ViewOffsets vo = view_offsets(nu, nv);
     const float inv_dz = 1.0f / h.dz;
     const float fnv = (float)nv;
-    const long long istride = (long long)(nv + 1) * nu;
+    const int cstride = (nv + 1) * nu;   // cells per base view
     // orbit columns: (i, j), (j, n-1-i), (n-1-i, n-1-j), (n-1-j, i)
     auto ocx = [&](int k) { return k == 0 ? ixc : k == 1 ? iyc : k == 2 ? n1 - ixc : n1 - iyc; };
     auto ocy = [&](int k) { return k == 0 ? iyc : k == 1 ? n1 - ixc : k == 2 ? n1 - iyc : ixc; };
-    float acc[4][kMoZ];
+    // Sums in slot order: in quarter turn s4 of the set-up views, slot t
+    // (view w + t Q of a cell) belongs to orbit column (t - s4) & 3; the slots
+    // rotate by one between quarter turns, and after the fourth slot k holds
+    // column k.  accp[0][j] = slots 0, 1 of voxel j; accp[1][j] = slots 2, 3.
+    float2 accp[2][kMoZ];
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int j = 0; j < kMoZ; ++j) acc[k][j] = 0.0f;
+    for (int j = 0; j < kMoZ; ++j) accp[0][j] = accp[1][j] = make_float2(0.0f, 0.0f);
+    int s4 = 0;
+    // column k's value v into voxel j (k and j known at compile time)
+    auto addcol = [&](int k, int j, float v) {
+        const int t = (s4 + k) & 3;
+        accp[0][j].x += t == 0 ? v : 0.0f;
+        accp[0][j].y += t == 1 ? v : 0.0f;
+        accp[1][j].x += t == 2 ? v : 0.0f;
+        accp[1][j].y += t == 3 ? v : 0.0f;
+    };
 
 #pragma unroll 1
     for (int sv = 0; sv < nall; ++sv) {
+        if (sv > 0 && sv % Q == 0) {
+            // next quarter turn: slot t takes the sums of slot t - 1
+#pragma unroll
+            for (int j = 0; j < kMoZ; ++j) {
+                const float2 a = accp[0][j], b = accp[1][j];
+                accp[0][j] = make_float2(b.y, a.x);
+                accp[1][j] = make_float2(a.y, b.x);
+            }
+            ++s4;
+        }
+        const int w = sv - s4 * Q;   // base view: the cell of views w + t Q
         int pv[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int v = sv + k * Q;
-            pv[k] = v < nall ? v : v - nall;
-        }
+        for (int k = 0; k < 4; ++k) pv[k] = w + ((s4 + k) & 3) * Q;
         const float *__restrict__ pzp = T + h.off_zplane;
         const float *__restrict__ V = T + h.off_views + (long long)sv * h.view_stride;
         const int axis = (int)V[VF_AXIS];
@@ -1392,9 +1481,9 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
 #pragma unroll
                 for (int j = 0; j < kMoZ; ++j) {
                     if (l0 + j >= nz) continue;
-                    acc[k][j] += ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
+                    addcol(k, j, ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
                                : ak == 1 ? matched_voxel_view<1>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
-                                         : matched_voxel_view<2>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j);
+                                         : matched_voxel_view<2>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j));
                 }
             }
             continue;
@@ -1466,7 +1555,7 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             if (ncol < kMC) {
                 cand[0][ncol][tid] = __int_as_float(c);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) cand[1 + k][ncol][tid] = ovk[k] * gk[k] * wz;
+                for (int k = 0; k < 4; ++k) cand[1 + ((s4 + k) & 3)][ncol][tid] = ovk[k] * gk[k] * wz;
                 cand[5][ncol][tid] = tau;
                 cand[6][ncol][tid] = inv;
                 ++ncol;
@@ -1485,8 +1574,8 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
 #pragma unroll
                 for (int j = 0; j < kMoZ; ++j) {
                     if (l0 + j >= nz) continue;
-                    acc[k][j] += ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
-                                         : matched_voxel_view<1>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j);
+                    addcol(k, j, ak == 0 ? matched_voxel_view<0>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j)
+                                         : matched_voxel_view<1>(h, T, Vk, vo, Qk, ocx(k), ocy(k), l0 + j));
                 }
             }
             continue;
@@ -1497,33 +1586,42 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             // candidate m: the same row placement as bp_matched_column
             const int cm = __float_as_int(cand[0][m][tid]);
             const float tm = cand[5][m][tid], bm = cand[6][m][tid];
-            float wk[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) wk[k] = bm > 0.0f ? cand[1 + k][m][tid] : -cand[1 + k][m][tid];
+            const float sgn = bm > 0.0f ? 1.0f : -1.0f;
+            const float2 w01 = make_float2(sgn * cand[1][m][tid], sgn * cand[2][m][tid]);
+            const float2 w23 = make_float2(sgn * cand[3][m][tid], sgn * cand[4][m][tid]);
             const int R = min(max((int)floorf(fmaf((float)l0 - A, bm, -b0r)), 0), nv);
             const ZFrame zf = row_frame(A, tm, B0, dB, (float)R);
             const float d0 = ((float)l0 - zf.ibf) - zf.f;
             const float rlo = -(float)R, rhi = fnv - (float)R;
-            int coff[4];   // element offsets of the four views' column cm (< 2^31, checked by the host)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) coff[k] = pv[k] * (int)istride + cm;
-            float eprev[4];
+            // float4 offset of base view w's cell (row R, column cm) (< 2^31, checked by the host)
+            const int coff = (w * cstride + R * nu + cm) * 2;
+            float2 ep01, ep23;
 #pragma unroll
             for (int j = 0; j <= kMoZ; ++j) {
                 const float rr = fminf(fmaxf((d0 + (float)j) * bm, rlo), rhi);
                 float fr;
-                const int mr = R + floor_split(rr, &fr);
-                const int off = mr * nu;
+                const int mr = floor_split(rr, &fr);
                 const float fx = rr - fr;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const float2 a = __ldg(integ + (coff[k] + off));
-                    const float e = fmaf(a.y, fx, a.x);
-                    if (j > 0) acc[k][j - 1] = fmaf(e - eprev[k], wk[k], acc[k][j - 1]);
-                    eprev[k] = e;
+                const float4 *cell = integ + (coff + mr * nu * 2);
+                const float4 C = __ldg(cell), Y = __ldg(cell + 1);
+                const float2 fx2 = make_float2(fx, fx);
+                const float2 e01 = __ffma2_rn(make_float2(Y.x, Y.y), fx2, make_float2(C.x, C.y));
+                const float2 e23 = __ffma2_rn(make_float2(Y.z, Y.w), fx2, make_float2(C.z, C.w));
+                if (j > 0) {
+                    accp[0][j - 1] = __ffma2_rn(__fadd2_rn(e01, make_float2(-ep01.x, -ep01.y)), w01, accp[0][j - 1]);
+                    accp[1][j - 1] = __ffma2_rn(__fadd2_rn(e23, make_float2(-ep23.x, -ep23.y)), w23, accp[1][j - 1]);
                 }
+                ep01 = e01;
+                ep23 = e23;
             }
         }
+    }
+    // the fourth quarter turn's rotation: slot k holds column k
+#pragma unroll
+    for (int j = 0; j < kMoZ; ++j) {
+        const float2 a = accp[0][j], b = accp[1][j];
+        accp[0][j] = make_float2(b.y, a.x);
+        accp[1][j] = make_float2(a.y, b.x);
     }
     if (!live) return;
 #pragma unroll
@@ -1533,7 +1631,8 @@ bp_matched_orbit_kernel(const float *__restrict__ T, const float2 *__restrict__ 
             const int iz = l0 + j;
             if (iz < nz) {
                 float *dst = vol + ((long long)iz * n + ocy(k)) * n + ocx(k);
-                const float b = __fmul_rn(scale, acc[k][j]);
+                const float a = k == 0 ? accp[0][j].x : k == 1 ? accp[0][j].y : k == 2 ? accp[1][j].x : accp[1][j].y;
+                const float b = __fmul_rn(scale, a);
                 *dst = accumulate ? __fadd_rn(*dst, b) : b;
             }
         }
@@ -1955,22 +2054,28 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
     std::vector<int> broken;
     if (CTGB_WALK_NC >= 4 && view0 == 0 && nviews == p->nviews && chunk >= nviews && square &&
         (long long)p->nviews * (p->nv + 1) * p->nu < (1LL << 31) && quarter_turn_views(p, &broken)) {
-        const long long threads = (long long)p->nu * nviews;
+        // the four views of each base view interleaved per cell (the same
+        // bytes as nviews views of (C, y') pairs), the column tables after them
+        const int q = nviews / 4;
+        const long long threads = (long long)p->nu * q;
         float *tabs = reinterpret_cast<float *>(ws + (size_t)nviews * (p->nv + 1) * p->nu);
-        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, d_proj, ws, tabs, 0, nviews);
+        matched_integrate_orbit_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+            T, d_proj, reinterpret_cast<float4 *>(ws), tabs);
         const int hn = p->nx / 2;
         dim3 ogrid((hn + kMiTX - 1) / kMiTX, (hn + kMiTY - 1) / kMiTY, (p->nz + kMoZ - 1) / kMoZ);
-        bp_matched_orbit_kernel<<<ogrid, block, 0, s>>>(T, ws, tabs, d_proj, d_vol, scale, accumulate);
-        // the views of groups the orbit kernel skipped, one launch each
-        const int q = nviews / 4;
-        const size_t rows_elems = (size_t)(p->nv + 1) * p->nu;
+        bp_matched_orbit_kernel<<<ogrid, block, 0, s>>>(T, reinterpret_cast<const float4 *>(ws), tabs, d_proj, d_vol,
+                                                         scale, accumulate);
+        // the views of groups the orbit kernel skipped, one at a time: each
+        // integrated again, as (C, y') pairs, into the workspace's start (the
+        // orbit kernel has read it by then: same stream)
         dim3 grid1((p->nx + kMiTX - 1) / kMiTX, (p->ny + kMiTY - 1) / kMiTY, (p->nz + kMZ - 1) / kMZ);
         for (int g : broken)
             for (int k = 0; k < 4; ++k) {
                 const int v = g + k * q;
-                bp_matched_integ_kernel<<<grid1, block, 0, s>>>(
-                    T, ws + (size_t)v * rows_elems, tabs + (size_t)v * matched_tab_stride(p->nu),
-                    d_proj + (long long)v * p->nu * p->nv, d_vol, v, 1, scale, 1);
+                const float *pv = d_proj + (long long)v * p->nu * p->nv;
+                float *tab_v = tabs + (size_t)v * matched_tab_stride(p->nu);
+                matched_integrate_kernel<<<(unsigned)((p->nu + 255) / 256), 256, 0, s>>>(T, pv, ws, tab_v, v, 1);
+                bp_matched_integ_kernel<<<grid1, block, 0, s>>>(T, ws, tab_v, pv, d_vol, v, 1, scale, 1);
             }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_orbit_kernel: %s", cudaGetErrorString(e));
