@@ -1148,49 +1148,47 @@ __device__ __forceinline__ void matched_integrate_one(const float *__restrict__ 
     o[(long long)nv * nu] = make_float2((float)run, 0.0f);
 }
 
-// The integration pass for the quarter-turn orbit kernel: thread (w, c)
-// integrates column c of the four views w + k Q (Q = views / 4) and writes,
-// per row boundary r, one 32-byte cell {C_0..C_3, y'_0..y'_3} at
-// ((w * (nv + 1) + r) * nu + c), so the orbit kernel's four lookups of a row
-// boundary are two adjacent 16-byte loads.  Values and tables as
-// matched_integrate_one (the same expressions per view).
+// The integration pass for the quarter-turn orbit kernel: per row boundary
+// r, one 32-byte cell {C_0..C_3, y'_0..y'_3} at ((w * (nv + 1) + r) * nu + c)
+// holds column c of the four views w + k Q (Q = views / 4), so the orbit
+// kernel's four lookups of a row boundary are two adjacent 16-byte loads.
+// Thread 4 g + k integrates view w + k Q of cell column g = w * nu + c: the
+// four threads of a cell are neighbouring lanes, whose stores fill the same
+// sector.  Values and tables as matched_integrate_one (the same expressions
+// per view).
 __global__ void matched_integrate_orbit_kernel(const float *__restrict__ T, const float *__restrict__ proj,
-                                               float4 *__restrict__ out, float *__restrict__ tabs) {
+                                               float *__restrict__ out, float *__restrict__ tabs) {
     const TableHeader &h = header(T);
     const int nu = h.nu, nv = h.nv, Q = h.nviews / 4;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)nu * Q) return;
-    const int w = (int)(t / nu), c = (int)(t % nu);
+    if (t >= 4LL * nu * Q) return;
+    const int k = (int)(t & 3);
+    const long long g = t >> 2;
+    const int w = (int)(g / nu), c = (int)(g % nu), v = w + k * Q;
     const ViewOffsets vo = view_offsets(nu, nv);
-    MatchedColumn mc[4];
-    const float *__restrict__ q[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int v = w + k * Q;
-        const float *__restrict__ V = T + h.off_views + (long long)v * h.view_stride;
-        mc[k] = matched_column_setup(h, V, vo, c, tabs + (long long)v * matched_tab_stride(nu));
-        q[k] = proj + (long long)v * nu * nv + c;
-    }
-    float4 *__restrict__ o = out + ((long long)w * (nv + 1) * nu + c) * 2;
-    double run[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int r = 0; r < nv; ++r) {
-        float y[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float raw = __ldg(q[k] + (long long)r * nu);
-            y[k] = mc[k].axis == 2 ? raw : raw * mc[k].K(r);
+    const float *__restrict__ V = T + h.off_views + (long long)v * h.view_stride;
+    const MatchedColumn mc = matched_column_setup(h, V, vo, c, tabs + (long long)v * matched_tab_stride(nu));
+    const float *__restrict__ q = proj + (long long)v * nu * nv + c;
+    float *__restrict__ o = out + ((long long)w * (nv + 1) * nu + c) * 8 + k;
+    const long long rstride = (long long)nu * 8;
+    if (mc.axis == 2) {
+        for (int r = 0; r < nv; ++r) {
+            o[r * rstride] = 0.0f;
+            o[r * rstride + 4] = __ldg(q + (long long)r * nu);
         }
-        float4 *cell = o + (long long)r * nu * 2;
-        cell[0] = make_float4(mc[0].axis == 2 ? 0.0f : (float)run[0], mc[1].axis == 2 ? 0.0f : (float)run[1],
-                              mc[2].axis == 2 ? 0.0f : (float)run[2], mc[3].axis == 2 ? 0.0f : (float)run[3]);
-        cell[1] = make_float4(y[0], y[1], y[2], y[3]);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) run[k] += y[k];
+        o[nv * rstride] = 0.0f;
+        o[nv * rstride + 4] = 0.0f;
+        return;
     }
-    float4 *cell = o + (long long)nv * nu * 2;
-    cell[0] = make_float4(mc[0].axis == 2 ? 0.0f : (float)run[0], mc[1].axis == 2 ? 0.0f : (float)run[1],
-                          mc[2].axis == 2 ? 0.0f : (float)run[2], mc[3].axis == 2 ? 0.0f : (float)run[3]);
-    cell[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    double run = 0.0;
+    for (int r = 0; r < nv; ++r) {
+        const float y = __ldg(q + (long long)r * nu) * mc.K(r);
+        o[r * rstride] = (float)run;
+        o[r * rstride + 4] = y;
+        run += y;
+    }
+    o[nv * rstride] = (float)run;
+    o[nv * rstride + 4] = 0.0f;
 }
 
 __global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
@@ -2057,10 +2055,10 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
         // the four views of each base view interleaved per cell (the same
         // bytes as nviews views of (C, y') pairs), the column tables after them
         const int q = nviews / 4;
-        const long long threads = (long long)p->nu * q;
+        const long long threads = 4LL * p->nu * q;
         float *tabs = reinterpret_cast<float *>(ws + (size_t)nviews * (p->nv + 1) * p->nu);
         matched_integrate_orbit_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-            T, d_proj, reinterpret_cast<float4 *>(ws), tabs);
+            T, d_proj, reinterpret_cast<float *>(ws), tabs);
         const int hn = p->nx / 2;
         dim3 ogrid((hn + kMiTX - 1) / kMiTX, (hn + kMiTY - 1) / kMiTY, (p->nz + kMoZ - 1) / kMoZ);
         bp_matched_orbit_kernel<<<ogrid, block, 0, s>>>(T, reinterpret_cast<const float4 *>(ws), tabs, d_proj, d_vol,
