@@ -207,6 +207,7 @@ struct ParamSrc {
     const float *tabs_, *proj_;
     int view0_, nviews_;
     float scale_;
+    int vstep_ = 1;   // view vi of the call is view0 + vi * vstep (integ: slot vi)
     __device__ __forceinline__ const float *T() const { return T_; }
     __device__ __forceinline__ const float2 *integ() const { return integ_; }
     __device__ __forceinline__ const float *tabs() const { return tabs_; }
@@ -214,6 +215,7 @@ struct ParamSrc {
     __device__ __forceinline__ int view0() const { return view0_; }
     __device__ __forceinline__ int nviews() const { return nviews_; }
     __device__ __forceinline__ float scale() const { return scale_; }
+    __device__ __forceinline__ int vstep() const { return vstep_; }
 };
 
 __device__ __forceinline__ unsigned long long ld_volatile_u64(const void *p) {
@@ -243,6 +245,7 @@ struct JobSrc {
     __device__ __forceinline__ int view0() const { return (int)ld_volatile_u32(&jp->view0); }
     __device__ __forceinline__ int nviews() const { return (int)ld_volatile_u32(&jp->nviews); }
     __device__ __forceinline__ float scale() const { return __uint_as_float(ld_volatile_u32(&jp->scale)); }
+    __device__ __forceinline__ int vstep() const { return 1; }
 };
 
 // CTA (bx, by, bz) of the FDK backprojection over integrated projections:
@@ -1121,19 +1124,22 @@ __device__ __forceinline__ MatchedColumn matched_column_setup(const TableHeader 
     return mc;
 }
 
-// Column c of view vi (t = vi * nu + c) of the matched backprojector's
-// integration pass.
+// Column c of the call's view vi (t = vi * nu + c; view view0 + vi * vstep,
+// its projections at proj + vi * vstep views, its table at tabs + vi * vstep
+// tables, its integrated rows in slot vi of out) of the matched
+// backprojector's integration pass.
 __device__ __forceinline__ void matched_integrate_one(const float *__restrict__ T, const float *__restrict__ proj,
                                                       float2 *__restrict__ out, float *__restrict__ tabs, int view0,
-                                                      long long t) {
+                                                      int vstep, long long t) {
     const TableHeader &h = header(T);
     const int nu = h.nu, nv = h.nv;
     const int vi = (int)(t / nu), c = (int)(t % nu);
     const ViewOffsets vo = view_offsets(nu, nv);
-    const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi) * h.view_stride;
-    const float *__restrict__ q = proj + (long long)vi * nu * nv + c;
+    const float *__restrict__ V = T + h.off_views + (long long)(view0 + vi * vstep) * h.view_stride;
+    const float *__restrict__ q = proj + (long long)vi * vstep * nu * nv + c;
     float2 *__restrict__ o = out + (long long)vi * (nv + 1) * nu + c;
-    const MatchedColumn mc = matched_column_setup(h, V, vo, c, tabs + (long long)vi * matched_tab_stride(nu));
+    const MatchedColumn mc =
+        matched_column_setup(h, V, vo, c, tabs + (long long)vi * vstep * matched_tab_stride(nu));
     if (mc.axis == 2) {
         for (int r = 0; r < nv; ++r) o[(long long)r * nu] = make_float2(0.0f, __ldg(q + (long long)r * nu));
         o[(long long)nv * nu] = make_float2(0.0f, 0.0f);
@@ -1193,10 +1199,10 @@ __global__ void matched_integrate_orbit_kernel(const float *__restrict__ T, cons
 
 __global__ void matched_integrate_kernel(const float *__restrict__ T, const float *__restrict__ proj,
                                          float2 *__restrict__ out, float *__restrict__ tabs, int view0,
-                                         int nviews) {
+                                         int nviews, int vstep) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)header(T).nu * nviews) return;
-    matched_integrate_one(T, proj, out, tabs, view0, t);
+    matched_integrate_one(T, proj, out, tabs, view0, vstep, t);
 }
 
 constexpr int kMC = 6;   // detector columns kept per (voxel column, view); more -> per-voxel path
@@ -1240,10 +1246,10 @@ __device__ __forceinline__ void bp_matched_column(const Src &src, int bx, int by
         const float *__restrict__ T = src.T();
         const TableHeader &h = header(T);
         const float *__restrict__ pzp = T + h.off_zplane;
-        const float *__restrict__ V = T + h.off_views + (long long)(src.view0() + vi) * h.view_stride;
+        const float *__restrict__ V = T + h.off_views + (long long)(src.view0() + vi * src.vstep()) * h.view_stride;
         const float2 *__restrict__ IQ = src.integ() + (long long)vi * (nv + 1) * nu;
         const int axis = (int)V[VF_AXIS];
-        const float *__restrict__ Qraw = src.proj() + (long long)vi * nu * nv;
+        const float *__restrict__ Qraw = src.proj() + (long long)vi * src.vstep() * nu * nv;
         if (axis == 2) {
             // z-dominant: per-voxel candidate search on the raw values.
             if (!live) continue;
@@ -1280,7 +1286,7 @@ __device__ __forceinline__ void bp_matched_column(const Src &src, int bx, int by
         const int cA = max((int)floorf(cmin) - 1, 0), cB = min((int)floorf(cmax) + 1, nu - 1);
         const float kf = (float)k;
         // Up to kMC columns with ov_x > 0 (the same x' expressions as the forward).
-        const float *__restrict__ EbT = src.tabs() + (long long)vi * matched_tab_stride(nu);
+        const float *__restrict__ EbT = src.tabs() + (long long)vi * src.vstep() * matched_tab_stride(nu);
         const float *__restrict__ IPT = EbT + nu + 1;
         int ncol = 0;
         int cc[kMC];
@@ -1361,8 +1367,8 @@ __device__ __forceinline__ void bp_matched_column(const Src &src, int bx, int by
 __global__ void __launch_bounds__(kMiTX * kMiTY, CTGB_MI_BLOCKS)
 bp_matched_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ integ,
                         const float *__restrict__ tabs, const float *__restrict__ proj, float *__restrict__ vol,
-                        int view0, int nviews, float scale, int accumulate) {
-    const ParamSrc src = {T, integ, tabs, proj, view0, nviews, scale};
+                        int view0, int nviews, float scale, int accumulate, int vstep) {
+    const ParamSrc src = {T, integ, tabs, proj, view0, nviews, scale, vstep};
     bp_matched_column(src, blockIdx.x, blockIdx.y, blockIdx.z,
                       [=](long long i, float a) {
                           const float b = __fmul_rn(scale, a);
@@ -1712,7 +1718,7 @@ __global__ void integrate_batch_kernel(const IntegJob *__restrict__ jobs, int nj
             else hi = mid - 1;
         }
         const IntegJob &jb = jobs[lo];
-        if (MATCHED) matched_integrate_one(jb.T, jb.proj, jb.out, jb.tabs, jb.view0, t - jb.t0);
+        if (MATCHED) matched_integrate_one(jb.T, jb.proj, jb.out, jb.tabs, jb.view0, 1, t - jb.t0);
         else integrate_rows_one(jb.proj, jb.out, jb.nu, jb.nv, t - jb.t0);
     }
 }
@@ -2063,18 +2069,17 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
         dim3 ogrid((hn + kMiTX - 1) / kMiTX, (hn + kMiTY - 1) / kMiTY, (p->nz + kMoZ - 1) / kMoZ);
         bp_matched_orbit_kernel<<<ogrid, block, 0, s>>>(T, reinterpret_cast<const float4 *>(ws), tabs, d_proj, d_vol,
                                                          scale, accumulate);
-        // the views of groups the orbit kernel skipped, one at a time: each
+        // the groups the orbit kernel skipped: the four views g + k q of each
         // integrated again, as (C, y') pairs, into the workspace's start (the
-        // orbit kernel has read it by then: same stream)
+        // orbit kernel has read it by then: same stream), then backprojected
+        // by one launch (view step q)
         dim3 grid1((p->nx + kMiTX - 1) / kMiTX, (p->ny + kMiTY - 1) / kMiTY, (p->nz + kMZ - 1) / kMZ);
-        for (int g : broken)
-            for (int k = 0; k < 4; ++k) {
-                const int v = g + k * q;
-                const float *pv = d_proj + (long long)v * p->nu * p->nv;
-                float *tab_v = tabs + (size_t)v * matched_tab_stride(p->nu);
-                matched_integrate_kernel<<<(unsigned)((p->nu + 255) / 256), 256, 0, s>>>(T, pv, ws, tab_v, v, 1);
-                bp_matched_integ_kernel<<<grid1, block, 0, s>>>(T, ws, tab_v, pv, d_vol, v, 1, scale, 1);
-            }
+        for (int g : broken) {
+            const float *pg = d_proj + (long long)g * p->nu * p->nv;
+            float *tab_g = tabs + (size_t)g * matched_tab_stride(p->nu);
+            matched_integrate_kernel<<<(unsigned)((4 * p->nu + 255) / 256), 256, 0, s>>>(T, pg, ws, tab_g, g, 4, q);
+            bp_matched_integ_kernel<<<grid1, block, 0, s>>>(T, ws, tab_g, pg, d_vol, g, 4, scale, 1, q);
+        }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_orbit_kernel: %s", cudaGetErrorString(e));
         return CTGB_OK;
@@ -2086,9 +2091,9 @@ extern "C" int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_t
         const float *pv = d_proj + (long long)v * p->nu * p->nv;
         // the chunk's n views of integrated rows, then their column tables
         float *tabs = reinterpret_cast<float *>(ws + (size_t)n * (p->nv + 1) * p->nu);
-        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, pv, ws, tabs, view0 + v, n);
+        matched_integrate_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(T, pv, ws, tabs, view0 + v, n, 1);
         const int acc = (v > 0) ? 1 : accumulate;
-        bp_matched_integ_kernel<<<grid, block, 0, s>>>(T, ws, tabs, pv, d_vol, view0 + v, n, scale, acc);
+        bp_matched_integ_kernel<<<grid, block, 0, s>>>(T, ws, tabs, pv, d_vol, view0 + v, n, scale, acc, 1);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTGB_ERR_CUDA, "bp_matched_integ_kernel: %s", cudaGetErrorString(e));
