@@ -461,22 +461,26 @@ constexpr int kWkTX = 4, kWkTY = 32, kWkThreads = kWkTX * kWkTY;   // 4 x 32 col
 // the code outgrew the instruction cache (stalls on instruction fetch were
 // the largest stall reason) and 96 registers still spilled.
 template <int NC> struct WalkShape;
-template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8; };
-template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8; };
+template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8, UNROLL = 1; };
+template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8, UNROLL = 1; };
 // Quarter-turn orbits: at 512^3 / 720 views, with the columns paired into
 // f32x2 lanes, the local voxel integrals and the row steps written out,
 // Z = 14 at 7 CTAs per SM takes 106.9 ms (Z = 16 at 6: 111.2; Z = 12 at 8:
-// 107.6; Z = 13 or 15 at 7: 107.8, 107.4; Z = 20 at 5: 120.3).  A longer
-// chunk shares each (column, view) set-up between more voxels, fewer
-// resident warps hide less of the row loads' latency.  (The running-sum walk
-// with a counted step loop: Z = 16 at 6 121.0 ms.)
+// 107.6; Z = 13 or 15 at 7: 107.8, 107.4; Z = 20 at 5: 120.3), and with the
+// voxel loop unrolled by 2 104.5 ms (by 7: 111.1; by 14 it spills: 191.9).
+// A longer chunk shares each (column, view) set-up between more voxels,
+// fewer resident warps hide less of the row loads' latency.  (The
+// running-sum walk with a counted step loop: Z = 16 at 6 121.0 ms.)
 #ifndef CTGB_WALK_Z4
 #define CTGB_WALK_Z4 14
 #endif
 #ifndef CTGB_WALK_B4
 #define CTGB_WALK_B4 7
 #endif
-template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = CTGB_WALK_B4; };
+#ifndef CTGB_WALK_U4
+#define CTGB_WALK_U4 2
+#endif
+template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = CTGB_WALK_B4, UNROLL = CTGB_WALK_U4; };
 
 // Walk rows upwards through one chunk of Z voxels for NC column-views.
 // vb[k]: view k's projections at column lbase, row 0.  Voxel j's footprint
@@ -488,10 +492,6 @@ template <> struct WalkShape<4> { static constexpr int Z = CTGB_WALK_Z4, MINB = 
 // at -y, as in every reference script, rows grow with the voxel index: row
 // coordinates run opposite to z on both axes.)  Voxel j of column k adds
 // into sacc[j * NC * kWkThreads + k] (sacc: this thread's slots).
-#ifndef CTGB_WALK_UNROLL
-#define CTGB_WALK_UNROLL 1
-#endif
-constexpr int kWalkUnroll = CTGB_WALK_UNROLL;
 template <int NC, int Z, int NT, bool CLAMP>
 __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, int nv, const float (&ov)[4],
                                           bool lin, float lo0, float hi0, float dlo, float dhi,
@@ -538,7 +538,7 @@ __device__ __forceinline__ void walk_rows(const float *const (&vb)[NC], int nu, 
         }
         rows(cur + 1, roff + nu, Rn);
     };
-#pragma unroll (kWalkUnroll)
+#pragma unroll (WalkShape<NC>::UNROLL)
     for (int j = 0; j < Z; ++j) {
         const float2 p = pos(j);
         const float rw = fast_rcp(p.y - p.x);
@@ -614,7 +614,7 @@ __device__ __forceinline__ void walk_rows_packed(const float *__restrict__ proj,
         }
         rows(cur + 1, roff + nu, Rn);
     };
-#pragma unroll (kWalkUnroll)
+#pragma unroll (WalkShape<NC>::UNROLL)
     for (int j = 0; j < Z; ++j) {
         const float2 p = pos(j);
         const float rw = fast_rcp(p.y - p.x);
