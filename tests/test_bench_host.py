@@ -27,7 +27,7 @@ def test_clock_summary_without_a_sampler_is_none():
 
 
 def test_profiled_traffic_reads_the_committed_summaries():
-    assert bench.profiled_traffic("bp_fdk_walk_kernel", "dd_pair") == 3.635e9
+    assert bench.profiled_traffic("bp_fdk_walk_kernel", "dd_pair") == 3.66e9
     assert bench.profiled_traffic("dd_forward_tma_kernel", "dd_pair") == 2.38e9
     assert bench.profiled_traffic("bp_fdk_integ_kernel", "dd384") == 7.63e9
     # another workload's capture is not borrowed
