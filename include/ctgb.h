@@ -171,7 +171,13 @@ int ctgb_backproject_matched(const ctgb_params *p, const void *d_table, const fl
  * factor and integrated along v into a caller-supplied workspace, with a
  * per-view table of the forward's detector-column slopes and depth factors
  * after them (size per view from ctgb_backproject_fdk_workspace_bytes, which
- * counts both), processed in view chunks that fit. */
+ * counts both), processed in view chunks that fit.  A call over every view of
+ * a quarter-turn-symmetric orbit (the conditions ctgb_backproject_fdk_orbit_size
+ * reports as 4, plus forward planes centred on the axis) whose views all fit
+ * takes one integration pass that stores the four views of each quarter-turn
+ * orbit side by side per detector cell, one orbit-kernel launch, and one
+ * launch per 45-degree group of views (whose dominant axes do not
+ * alternate); the result is the chunked path's up to float summation order. */
 int ctgb_backproject_matched_ws(const ctgb_params *p, const void *d_table, const float *d_proj, float *d_vol,
                                 int32_t view0, int32_t nviews, float scale, int32_t accumulate, void *d_workspace,
                                 size_t workspace_bytes, void *stream);
