@@ -455,11 +455,12 @@ bp_fdk_integ_kernel(const float *__restrict__ T, const float2 *__restrict__ inte
 // footprint is computed once and serves four column-views, whose rows are
 // walked side by side.
 constexpr int kWkTX = 4, kWkTY = 32, kWkThreads = kWkTX * kWkTY;   // 4 x 32 columns per CTA, 4 x 8 per warp
-// Z voxels per column chunk and resident CTAs per SM.  The voxel sums live in
-// shared memory (Z * NC floats per thread, each thread its own slots), so the
-// voxel loop stays rolled: with the sums in registers and the loop unrolled,
-// the code outgrew the instruction cache (stalls on instruction fetch were
-// the largest stall reason) and 96 registers still spilled.
+// Z voxels per column chunk, resident CTAs per SM and the voxel loop's unroll
+// factor.  The voxel sums live in shared memory (Z * NC floats per thread,
+// each thread its own slots), so the voxel loop need not be unrolled: with
+// the sums in registers and the loop fully unrolled, the code outgrew the
+// instruction cache (stalls on instruction fetch were the largest stall
+// reason) and 96 registers still spilled.
 template <int NC> struct WalkShape;
 template <> struct WalkShape<1> { static constexpr int Z = 16, MINB = 8, UNROLL = 1; };
 template <> struct WalkShape<2> { static constexpr int Z = 16, MINB = 8, UNROLL = 1; };
