@@ -280,7 +280,9 @@ def run_ours(args):
     roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(kname, "dd_pair" if not args.small else "small"),
                 "algorithmic_bytes_per_launch": alg_bytes, "ms_per_launch": per_launch[dom],
-                "per_kernel_frac": {k: 4.0 * vv / (kern[k] / 1e3) / 1e9 / peak for k in ("forward", "backproject_fdk")}}
+                "per_kernel_frac": {k: 4.0 * vv / (kern[k] / 1e3) / 1e9 / peak for k in ("forward", "backproject_fdk")},
+                # the whole step (transpose, forward, backprojection): 4 B per voxel-view each way
+                "pair_frac": 2 * 4.0 * vv / (ms / 1e3) / 1e9 / peak}
 
     # matched pair (autograd path): forward + exact adjoint
     matched = None
