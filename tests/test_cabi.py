@@ -146,6 +146,34 @@ def test_fdk_orbit_size(over, nc):
     assert got.value == nc
 
 
+def test_backprojection_entry_points_reject_bad_arguments_on_the_host():
+    """The backprojection entry points check their arguments on the host and
+    return before any launch: NULL pointers, base or view ranges outside the
+    scan, a missing or too small workspace, and the bounded-wait self-test's
+    poll count.  The device pointers are placeholders that no failing call
+    reaches."""
+    c = ReconstructionParams.from_dict(cone_params(n=12, nviews=16, nu=20, nv=16), None).to_ctgb()
+    dev = ctypes.c_void_p(256)
+    nc = ctypes.c_int32(0)
+    _lib.call("ctgb_backproject_fdk_orbit_size", ctypes.byref(c), ctypes.byref(nc))
+    assert nc.value == 4
+    period = c.nviews // nc.value
+    with pytest.raises(ValueError, match="NULL argument"):
+        _lib.call("ctgb_backproject_fdk_orbits", ctypes.byref(c), None, dev, dev, 0, 1, 1.0, 0, None)
+    with pytest.raises(ValueError, match="base views"):
+        _lib.call("ctgb_backproject_fdk_orbits", ctypes.byref(c), dev, dev, dev, period - 1, 2, 1.0, 0, None)
+    with pytest.raises(ValueError, match="NULL workspace"):
+        _lib.call("ctgb_backproject_matched_ws", ctypes.byref(c), dev, dev, dev, 0, 1, 1.0, 0, None, 0, None)
+    with pytest.raises(ValueError, match="workspace below one view"):
+        _lib.call("ctgb_backproject_matched_ws", ctypes.byref(c), dev, dev, dev, 0, 1, 1.0, 0, dev, 16, None)
+    with pytest.raises(ValueError, match="view range"):
+        _lib.call("ctgb_backproject_matched_ws", ctypes.byref(c), dev, dev, dev, 0, c.nviews + 1, 1.0, 0, dev,
+                  1 << 30, None)
+    for polls in (0, (1 << 20) + 1):
+        with pytest.raises(ValueError, match="polls"):
+            _lib.call("ctgb_selftest_bounded_wait", polls, None)
+
+
 def test_table_rejects_bad_geometry():
     p = ReconstructionParams.from_dict(cone_params()).to_ctgb()
     p.nu = 0
